@@ -1,0 +1,133 @@
+/*
+ * smuthi_gb300 -- C ABI of the GB300-native radial-lookup coupling solve path.
+ *
+ * Drop-in boundary for SMUTHI's CouplingMatrixRadialLookupCUDA and the GMRES
+ * loop that drives it. Every entry point returns an int status (SG_OK = 0);
+ * no exception crosses the ABI. Host buffers are owned by the caller and are
+ * read or written only during the call; device buffers are owned by the
+ * context. One context serves one host thread at a time.
+ *
+ * Complex numbers are interleaved (re, im) pairs of double. A "system vector"
+ * uses the reference layout: particle-major, each particle's block ordered
+ * by its own multi index n(tau, l, m) (smuthi/fields/__init__.py:29-80).
+ * Multi-RHS arrays are [unknown][rhs] (the rhs index runs fastest).
+ */
+#ifndef SMUTHI_GB300_H
+#define SMUTHI_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SG_OK 0
+#define SG_ERR_ARG 1          /* invalid argument or call order */
+#define SG_ERR_CUDA 2         /* CUDA runtime error or out of device memory */
+#define SG_ERR_NOT_CONVERGED 3 /* solver hit its iteration limit; outputs hold the last iterate */
+#define SG_ERR_NAN 4          /* NaN/Inf detected in an input or an iterate */
+#define SG_ERR_NO_DEVICE 5    /* no CUDA device available */
+
+/* lookup interpolation kinds */
+#define SG_LINEAR 0           /* scipy interp1d(kind='linear') */
+#define SG_CUBIC 1            /* scipy interp1d(kind='cubic'): not-a-knot cubic spline */
+#define SG_CUBIC_HERMITE 2    /* 4-tap Catmull-Rom of the reference CUDA kernel */
+
+/* arithmetic of an operator application */
+#define SG_FP64 0
+#define SG_FP32 1
+
+typedef struct sg_context sg_context;
+
+/* Text of the last error on the calling thread ("" if none). */
+const char *sg_last_error(void);
+
+/* Library version string. */
+const char *sg_version(void);
+
+/* Create / destroy a context on CUDA device `device`.
+ * Replaces the PyCUDA autoinit + gpuarray set-up of
+ * smuthi/linearsystem/linear_system.py:829-882. */
+int sg_create(int device, sg_context **out);
+int sg_destroy(sg_context *ctx);
+
+/* Particles and unknowns (smuthi/linearsystem/linear_system.py:848-869).
+ * xy[2*i+{0,1}]: particle i lateral position (all particles share one z).
+ * unknown_particle[u], unknown_n[u]: particle number and global lookup index
+ * n(tau, l, m; l_max, m_max) of system-vector entry u, u < n_unknowns.
+ * m_of_n[n]: multipole order m of global lookup index n, n < blocksize. */
+int sg_set_particles(sg_context *ctx, int n_particles, const double *xy, int n_unknowns,
+                     const int32_t *unknown_particle, const int32_t *unknown_n, int blocksize,
+                     const int32_t *m_of_n);
+
+/* Radial lookup table w[rho][n1][n2] (complex, len_rho x blocksize^2) on the
+ * grid rho_k = rho_min + k * resolution, with interpolation `kind`.
+ * Replaces the table upload and kernel compile of
+ * smuthi/linearsystem/linear_system.py:838-881 (which cast to float32);
+ * the table is kept in FP64 and also rounded once to FP32 for SG_FP32. */
+int sg_set_lookup(sg_context *ctx, int kind, int len_rho, double rho_min, double resolution,
+                  const double *table);
+
+/* Per-particle T-matrices (smuthi/linearsystem/linear_system.py:410-424):
+ * n_types distinct blocks t[type][n1][n2] in the global lookup index space
+ * (blocksize x blocksize complex); particle_type[i] picks particle i's block.
+ * diagonal != 0 declares every block diagonal (Mie spheres). */
+int sg_set_tmatrix(sg_context *ctx, int n_types, const double *t, const int32_t *particle_type, int diagonal);
+
+/* y = W x, the coupling matvec (host buffers, n_unknowns x nrhs complex).
+ * Replaces CouplingMatrixRadialLookupCUDA.linear_operator.matvec,
+ * smuthi/linearsystem/linear_system.py:888-900. */
+int sg_coupling_matvec(sg_context *ctx, const double *x, double *y, int nrhs, int precision);
+
+/* y = x - T W x, the master operator (smuthi/linearsystem/linear_system.py:402-407). */
+int sg_master_matvec(sg_context *ctx, const double *x, double *y, int nrhs, int precision);
+
+/* Device-pointer variants: x, y are device buffers in the reference layout;
+ * `stream` is a cudaStream_t (NULL = the context's stream). Asynchronous. */
+int sg_coupling_matvec_dev(sg_context *ctx, const void *x, void *y, int nrhs, int precision, void *stream);
+int sg_master_matvec_dev(sg_context *ctx, const void *x, void *y, int nrhs, int precision, void *stream);
+
+/* Solver report. */
+typedef struct sg_solve_info {
+  int32_t iterations;      /* inner (Arnoldi) iterations, max over rhs */
+  int32_t restarts;        /* restart cycles (plain) or refinement steps (mixed) */
+  int32_t fp64_matvecs;    /* FP64 operator applications */
+  int32_t fp32_matvecs;    /* FP32 operator applications */
+  int32_t converged;       /* number of rhs that met the tolerance */
+  int32_t reserved;
+  double max_rel_residual; /* max over rhs of ||b - M x|| / ||b|| (FP64 operator) */
+  double seconds;          /* wall time of the solve on the device */
+} sg_solve_info;
+
+/* GMRES(restart) on the master operator, scipy semantics of the call at
+ * smuthi/linearsystem/linear_system.py:285 (x0 = given x, restart default 20,
+ * stop when ||b - M x|| <= rtol ||b||, explicit residual at every restart).
+ * b, x: host buffers n_unknowns x nrhs; x holds x0 on entry and the solution
+ * on return. nrhs > 1 runs independent Krylov spaces in lockstep, sharing one
+ * block matvec per iteration. precision = SG_FP64 (plain drop-in) or
+ * SG_FP32 (mixed: FP32 operator inside FP64 iterative refinement with FP64
+ * true residuals and FP64 Arnoldi). maxiter <= 0 selects 10 * n_unknowns. */
+int sg_gmres_solve(sg_context *ctx, const double *b, double *x, int nrhs, double rtol, int restart,
+                   int maxiter, int precision, sg_solve_info *info);
+
+/* Device-pointer variant of sg_gmres_solve (b, x device buffers). */
+int sg_gmres_solve_dev(sg_context *ctx, const void *b, void *x, int nrhs, double rtol, int restart,
+                       int maxiter, int precision, sg_solve_info *info, void *stream);
+
+/* ||b - M x|| / ||b|| per rhs with the FP64 operator (host buffers). */
+int sg_true_residual(sg_context *ctx, const double *b, const double *x, int nrhs, double *rel_residual);
+
+/* Kernel instrumentation. sg_profile(ctx, 1) brackets every coupling-kernel
+ * launch with CUDA events on its stream; sg_kernel_timing synchronises and
+ * returns the summed event time (ms) and the number of bracketed launches
+ * since the last reset. sg_launch_count returns the number of kernels this
+ * context has launched since it was created. */
+int sg_profile(sg_context *ctx, int enable);
+int sg_kernel_timing(sg_context *ctx, double *total_ms, int64_t *count, int reset);
+int sg_launch_count(sg_context *ctx, int64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SMUTHI_GB300_H */

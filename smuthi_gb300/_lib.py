@@ -1,0 +1,214 @@
+"""ctypes binding of the in-tree CUDA library ``libsmuthi_gb300.so``.
+
+The library is the only compute path of this package: there is no CPU
+fallback. ``lib()`` raises ``LibraryMissing`` when the shared object has not
+been built (``python -m smuthi_gb300.build``) and every wrapped call raises
+``SmuthiGB300Error`` with the library's message when it returns a non-zero
+status.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsmuthi_gb300.so")
+
+SG_OK, SG_ERR_ARG, SG_ERR_CUDA, SG_ERR_NOT_CONVERGED, SG_ERR_NAN, SG_ERR_NO_DEVICE = range(6)
+SG_LINEAR, SG_CUBIC, SG_CUBIC_HERMITE = 0, 1, 2
+SG_FP64, SG_FP32 = 0, 1
+KINDS = {"linear": SG_LINEAR, "cubic": SG_CUBIC, "cubic_hermite": SG_CUBIC_HERMITE}
+
+#: every entry point declared in include/smuthi_gb300.h
+EXPORTS = ("sg_last_error", "sg_version", "sg_create", "sg_destroy", "sg_set_particles", "sg_set_lookup",
+           "sg_set_tmatrix", "sg_coupling_matvec", "sg_master_matvec", "sg_coupling_matvec_dev",
+           "sg_master_matvec_dev", "sg_gmres_solve", "sg_gmres_solve_dev", "sg_true_residual", "sg_profile",
+           "sg_kernel_timing", "sg_launch_count")
+
+
+class LibraryMissing(RuntimeError):
+    pass
+
+
+class SmuthiGB300Error(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__("smuthi_gb300 error %d: %s" % (code, message))
+        self.code = code
+
+
+class NotConverged(SmuthiGB300Error):
+    pass
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("restarts", ctypes.c_int32), ("fp64_matvecs", ctypes.c_int32),
+                ("fp32_matvecs", ctypes.c_int32), ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("max_rel_residual", ctypes.c_double), ("seconds", ctypes.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
+_LIB = None
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+
+
+def _declare(L):
+    L.sg_last_error.restype = ctypes.c_char_p
+    L.sg_version.restype = ctypes.c_char_p
+    sigs = {
+        "sg_create": [_I, ctypes.POINTER(_P)],
+        "sg_destroy": [_P],
+        "sg_set_particles": [_P, _I, _P, _I, _P, _P, _I, _P],
+        "sg_set_lookup": [_P, _I, _I, _D, _D, _P],
+        "sg_set_tmatrix": [_P, _I, _P, _P, _I],
+        "sg_coupling_matvec": [_P, _P, _P, _I, _I],
+        "sg_master_matvec": [_P, _P, _P, _I, _I],
+        "sg_coupling_matvec_dev": [_P, _P, _P, _I, _I, _P],
+        "sg_master_matvec_dev": [_P, _P, _P, _I, _I, _P],
+        "sg_gmres_solve": [_P, _P, _P, _I, _D, _I, _I, _I, ctypes.POINTER(SolveInfo)],
+        "sg_gmres_solve_dev": [_P, _P, _P, _I, _D, _I, _I, _I, ctypes.POINTER(SolveInfo), _P],
+        "sg_true_residual": [_P, _P, _P, _I, _P],
+        "sg_profile": [_P, _I],
+        "sg_kernel_timing": [_P, ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_int64), _I],
+        "sg_launch_count": [_P, ctypes.POINTER(ctypes.c_int64)],
+    }
+    for name, args in sigs.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = _I
+
+
+def lib():
+    """Load (once) and return the ctypes library handle."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise LibraryMissing("CUDA library not built: %s is missing (run python -m smuthi_gb300.build)"
+                                 % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        _declare(L)
+        _LIB = L
+    return _LIB
+
+
+def check(rc):
+    if rc != SG_OK:
+        msg = lib().sg_last_error().decode(errors="replace")
+        if rc == SG_ERR_NOT_CONVERGED:
+            raise NotConverged(rc, msg)
+        raise SmuthiGB300Error(rc, msg)
+
+
+def ptr(a):
+    """Pointer to the data of a C-contiguous numpy array."""
+    assert a.flags["C_CONTIGUOUS"], "array must be C-contiguous"
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """Owns one ``sg_context`` on a CUDA device."""
+
+    def __init__(self, device=0):
+        L = lib()
+        h = ctypes.c_void_p()
+        check(L.sg_create(device, ctypes.byref(h)))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            lib().sg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- uploads
+    def set_particles(self, xy, unknown_particle, unknown_n, blocksize, m_of_n):
+        xy = np.ascontiguousarray(xy, dtype=np.float64)
+        up = np.ascontiguousarray(unknown_particle, dtype=np.int32)
+        un = np.ascontiguousarray(unknown_n, dtype=np.int32)
+        mo = np.ascontiguousarray(m_of_n, dtype=np.int32)
+        check(lib().sg_set_particles(self.h, xy.shape[0], ptr(xy), len(up), ptr(up), ptr(un), int(blocksize),
+                                     ptr(mo)))
+
+    def set_lookup(self, kind, table, rho_min, resolution):
+        tab = np.ascontiguousarray(table, dtype=np.complex128)
+        check(lib().sg_set_lookup(self.h, KINDS[kind] if isinstance(kind, str) else int(kind), tab.shape[0],
+                                  float(rho_min), float(resolution), ptr(tab)))
+
+    def set_tmatrix(self, blocks, particle_type, diagonal):
+        t = np.ascontiguousarray(blocks, dtype=np.complex128)
+        pt = np.ascontiguousarray(particle_type, dtype=np.int32)
+        check(lib().sg_set_tmatrix(self.h, t.shape[0], ptr(t), ptr(pt), 1 if diagonal else 0))
+
+    # -- operators (host buffers)
+    def _matvec(self, fn, x, precision):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        nrhs = 1 if x.ndim == 1 else x.shape[1]
+        y = np.empty_like(x)
+        check(fn(self.h, ptr(x), ptr(y), nrhs, precision))
+        return y
+
+    def coupling_matvec(self, x, precision=SG_FP64):
+        return self._matvec(lib().sg_coupling_matvec, x, precision)
+
+    def master_matvec(self, x, precision=SG_FP64):
+        return self._matvec(lib().sg_master_matvec, x, precision)
+
+    def gmres(self, b, x0, rtol, restart=20, maxiter=0, precision=SG_FP64, raise_on_failure=True):
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.array(x0, dtype=np.complex128, order="C", copy=True)
+        nrhs = 1 if b.ndim == 1 else b.shape[1]
+        info = SolveInfo()
+        rc = lib().sg_gmres_solve(self.h, ptr(b), ptr(x), nrhs, float(rtol), int(restart), int(maxiter),
+                                  int(precision), ctypes.byref(info))
+        if rc != SG_OK and (raise_on_failure or rc != SG_ERR_NOT_CONVERGED):
+            check(rc)
+        return x, info
+
+    def gmres_dev(self, b_ptr, x_ptr, nrhs, rtol, restart=20, maxiter=0, precision=SG_FP64, stream=None):
+        info = SolveInfo()
+        rc = lib().sg_gmres_solve_dev(self.h, ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr), int(nrhs),
+                                      float(rtol), int(restart), int(maxiter), int(precision), ctypes.byref(info),
+                                      ctypes.c_void_p(stream or 0))
+        if rc not in (SG_OK, SG_ERR_NOT_CONVERGED):
+            check(rc)
+        return info
+
+    def master_matvec_dev(self, x_ptr, y_ptr, nrhs, precision=SG_FP64, stream=None):
+        check(lib().sg_master_matvec_dev(self.h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr), int(nrhs),
+                                         int(precision), ctypes.c_void_p(stream or 0)))
+
+    def coupling_matvec_dev(self, x_ptr, y_ptr, nrhs, precision=SG_FP64, stream=None):
+        check(lib().sg_coupling_matvec_dev(self.h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr), int(nrhs),
+                                           int(precision), ctypes.c_void_p(stream or 0)))
+
+    def true_residual(self, b, x):
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        nrhs = 1 if b.ndim == 1 else b.shape[1]
+        out = np.zeros(nrhs)
+        check(lib().sg_true_residual(self.h, ptr(b), ptr(x), nrhs, ptr(out)))
+        return out
+
+    # -- instrumentation
+    def profile(self, enable=True):
+        check(lib().sg_profile(self.h, 1 if enable else 0))
+
+    def kernel_timing(self, reset=True):
+        ms = ctypes.c_double()
+        n = ctypes.c_int64()
+        check(lib().sg_kernel_timing(self.h, ctypes.byref(ms), ctypes.byref(n), 1 if reset else 0))
+        return ms.value, n.value
+
+    def launch_count(self):
+        n = ctypes.c_int64()
+        check(lib().sg_launch_count(self.h, ctypes.byref(n)))
+        return n.value

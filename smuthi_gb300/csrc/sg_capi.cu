@@ -1,0 +1,443 @@
+// C ABI of the smuthi_gb300 library: context, uploads, validation and entry points.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <string>
+#include <vector>
+
+#include "sg_internal.h"
+
+static thread_local std::string g_last_error;
+
+namespace sg {
+void set_error(const std::string &msg) { g_last_error = msg; }
+void clear_error() { g_last_error.clear(); }
+}  // namespace sg
+
+template <class F>
+static int guarded(F &&f) {
+  sg::clear_error();
+  try {
+    return f();
+  } catch (const sg::Error &e) {
+    sg::set_error(e.msg);
+    return e.code;
+  } catch (const std::exception &e) {
+    sg::set_error(std::string("internal error: ") + e.what());
+    return SG_ERR_CUDA;
+  } catch (...) {
+    sg::set_error("internal error");
+    return SG_ERR_CUDA;
+  }
+}
+
+static void use_device(sg_context *c) { SG_CUDA(cudaSetDevice(c->device)); }
+
+static void require_ready(sg_context *c, bool need_t) {
+  SG_REQUIRE(c != nullptr, "null context");
+  SG_REQUIRE(c->n > 0, "sg_set_particles has not been called");
+  SG_REQUIRE(c->kind >= 0, "sg_set_lookup has not been called");
+  if (need_t) SG_REQUIRE(c->t_ready, "sg_set_tmatrix has not been called");
+}
+
+static void ensure_pairs(sg_context *c, cudaStream_t st) {
+  if (c->pairs_ready) return;
+  c->pairs.reserve((size_t)c->n * c->n);
+  sg::build_pairs(c->pos.ptr, c->n, c->rho_min, c->res, c->n_int, c->pairs.ptr, st);
+  c->launches += 1;
+  c->pairs_ready = true;
+}
+
+static bool all_finite(const double *p, size_t n) {
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(p[i])) return false;
+  return true;
+}
+
+extern "C" {
+
+const char *sg_last_error(void) { return g_last_error.c_str(); }
+
+const char *sg_version(void) { return "smuthi_gb300 0.1 (sm_103a)"; }
+
+int sg_create(int device, sg_context **out) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(out != nullptr, "null output pointer");
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+      cudaGetLastError();
+      throw sg::Error{SG_ERR_NO_DEVICE, "no CUDA device available"};
+    }
+    SG_REQUIRE(device >= 0 && device < count, "device index out of range");
+    SG_CUDA(cudaSetDevice(device));
+    sg_context *c = new sg_context();
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete c;
+      throw sg::Error{SG_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)};
+    }
+    c->own_stream = true;
+    *out = c;
+    return SG_OK;
+  });
+}
+
+int sg_destroy(sg_context *ctx) {
+  return guarded([&]() -> int {
+    if (!ctx) return SG_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto &ev : ctx->events) {
+      cudaEventDestroy(ev.first);
+      cudaEventDestroy(ev.second);
+    }
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SG_OK;
+  });
+}
+
+int sg_set_particles(sg_context *ctx, int n_particles, const double *xy, int n_unknowns,
+                     const int32_t *unknown_particle, const int32_t *unknown_n, int blocksize,
+                     const int32_t *m_of_n) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx != nullptr, "null context");
+    SG_REQUIRE(n_particles >= 1, "need at least one particle");
+    SG_REQUIRE(blocksize >= 1 && blocksize <= 96, "blocksize must be in [1, 96]");
+    SG_REQUIRE(n_unknowns >= 1 && (long long)n_unknowns <= (long long)n_particles * blocksize,
+               "n_unknowns must be in [1, n_particles * blocksize]");
+    SG_REQUIRE(xy && unknown_particle && unknown_n && m_of_n, "null input array");
+    SG_REQUIRE(all_finite(xy, 2 * (size_t)n_particles), "particle positions must be finite");
+    use_device(ctx);
+    std::vector<char> seen((size_t)n_particles * blocksize, 0);
+    std::vector<int> map(n_unknowns);
+    bool uniform = (long long)n_unknowns == (long long)n_particles * blocksize;
+    for (int u = 0; u < n_unknowns; ++u) {
+      const int p = unknown_particle[u], n = unknown_n[u];
+      SG_REQUIRE(p >= 0 && p < n_particles, "unknown_particle out of range");
+      SG_REQUIRE(n >= 0 && n < blocksize, "unknown_n out of range");
+      const size_t pad = (size_t)p * blocksize + n;
+      SG_REQUIRE(!seen[pad], "duplicate (particle, n) pair in the unknown list");
+      seen[pad] = 1;
+      map[u] = (int)pad;
+      if ((size_t)u != pad) uniform = false;
+    }
+    int mmax = 0;
+    for (int n = 0; n < blocksize; ++n) mmax = std::max(mmax, std::abs((int)m_of_n[n]));
+    SG_REQUIRE(mmax <= 16, "|m| must be <= 16");
+    ctx->n = n_particles;
+    ctx->bs = blocksize;
+    ctx->n_unknowns = n_unknowns;
+    ctx->uniform = uniform;
+    std::vector<double2> pos(n_particles);
+    for (int i = 0; i < n_particles; ++i) pos[i] = make_double2(xy[2 * i], xy[2 * i + 1]);
+    ctx->pos.reserve(n_particles);
+    SG_CUDA(cudaMemcpy(ctx->pos.ptr, pos.data(), n_particles * sizeof(double2), cudaMemcpyHostToDevice));
+    ctx->h_mofn.assign(m_of_n, m_of_n + blocksize);
+    ctx->mofn.reserve(blocksize);
+    SG_CUDA(cudaMemcpy(ctx->mofn.ptr, ctx->h_mofn.data(), blocksize * sizeof(int), cudaMemcpyHostToDevice));
+    if (!uniform) {
+      ctx->map.reserve(n_unknowns);
+      SG_CUDA(cudaMemcpy(ctx->map.ptr, map.data(), n_unknowns * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    ctx->pairs_ready = false;
+    ctx->kind = -1;  // the table must be re-uploaded for a new geometry
+    ctx->t_ready = false;
+    return SG_OK;
+  });
+}
+
+int sg_set_lookup(sg_context *ctx, int kind, int len_rho, double rho_min, double resolution, const double *table) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx != nullptr, "null context");
+    SG_REQUIRE(ctx->n > 0, "sg_set_particles must precede sg_set_lookup");
+    SG_REQUIRE(kind == SG_LINEAR || kind == SG_CUBIC || kind == SG_CUBIC_HERMITE, "unknown interpolation kind");
+    SG_REQUIRE(len_rho >= (kind == SG_LINEAR ? 2 : 4), "lookup table too short for this interpolation kind");
+    SG_REQUIRE(resolution > 0 && std::isfinite(resolution) && std::isfinite(rho_min), "bad lookup grid");
+    SG_REQUIRE(table != nullptr, "null table");
+    const int bs = ctx->bs;
+    const size_t count = (size_t)len_rho * bs * bs;
+    if (!all_finite(table, 2 * count)) throw sg::Error{SG_ERR_NAN, "lookup table holds NaN or Inf"};
+    // the grid must cover every pair distance: largest rho must sit in an interval
+    std::vector<double2> pos(ctx->n);
+    use_device(ctx);
+    SG_CUDA(cudaMemcpy(pos.data(), ctx->pos.ptr, ctx->n * sizeof(double2), cudaMemcpyDeviceToHost));
+    double r2max = 0.0;
+    for (int i = 0; i < ctx->n; ++i)
+      for (int j = i + 1; j < ctx->n; ++j) {
+        const double dx = pos[i].x - pos[j].x, dy = pos[i].y - pos[j].y;
+        r2max = std::max(r2max, dx * dx + dy * dy);
+      }
+    const double rmax = std::sqrt(r2max);
+    const int need = kind == SG_CUBIC_HERMITE ? 3 : 2;
+    SG_REQUIRE(rho_min <= 0.0 && std::floor((rmax - rho_min) / resolution) + need <= len_rho,
+               "lookup grid does not cover [0, largest particle distance]");
+    const int ncoef = sg::coef_count(kind);
+    const int n_int = len_rho - 1;
+    cudaStream_t st = ctx->stream;
+    sg::DevBuf<double2> raw, work;
+    raw.reserve(count);
+    if (kind == SG_CUBIC) work.reserve(count);
+    SG_CUDA(cudaMemcpyAsync(raw.ptr, table, count * sizeof(double2), cudaMemcpyHostToDevice, st));
+    ctx->coef64.reserve((size_t)n_int * ncoef * bs * bs);
+    ctx->coef32.reserve((size_t)n_int * ncoef * bs * bs);
+    sg::build_coefficients(kind, raw.ptr, len_rho, bs, ctx->coef64.ptr, ctx->coef32.ptr, work.ptr, st);
+    ctx->launches += kind == SG_CUBIC ? 2 : 1;
+    ctx->kind = kind;
+    ctx->len_rho = len_rho;
+    ctx->n_int = n_int;
+    ctx->ncoef = ncoef;
+    ctx->rho_min = rho_min;
+    ctx->res = resolution;
+    ctx->pairs_ready = false;
+    return SG_OK;
+  });
+}
+
+int sg_set_tmatrix(sg_context *ctx, int n_types, const double *t, const int32_t *particle_type, int diagonal) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx != nullptr, "null context");
+    SG_REQUIRE(ctx->n > 0, "sg_set_particles must precede sg_set_tmatrix");
+    SG_REQUIRE(n_types >= 1 && t && particle_type, "bad T-matrix arguments");
+    const int bs = ctx->bs;
+    const size_t full = (size_t)n_types * bs * bs;
+    if (!all_finite(t, 2 * full)) throw sg::Error{SG_ERR_NAN, "T-matrix holds NaN or Inf"};
+    for (int i = 0; i < ctx->n; ++i)
+      SG_REQUIRE(particle_type[i] >= 0 && particle_type[i] < n_types, "particle_type out of range");
+    use_device(ctx);
+    const double2 *tc = reinterpret_cast<const double2 *>(t);
+    if (diagonal) {
+      std::vector<double2> d((size_t)n_types * bs);
+      for (int ty = 0; ty < n_types; ++ty)
+        for (int a = 0; a < bs; ++a) {
+          for (int b2 = 0; b2 < bs; ++b2)
+            if (b2 != a) {
+              const double2 v = tc[((size_t)ty * bs + a) * bs + b2];
+              SG_REQUIRE(v.x == 0.0 && v.y == 0.0, "T-matrix declared diagonal has off-diagonal entries");
+            }
+          d[(size_t)ty * bs + a] = tc[((size_t)ty * bs + a) * bs + a];
+        }
+      ctx->tmat.reserve(d.size());
+      SG_CUDA(cudaMemcpy(ctx->tmat.ptr, d.data(), d.size() * sizeof(double2), cudaMemcpyHostToDevice));
+    } else {
+      ctx->tmat.reserve(full);
+      SG_CUDA(cudaMemcpy(ctx->tmat.ptr, tc, full * sizeof(double2), cudaMemcpyHostToDevice));
+    }
+    ctx->ptype.reserve(ctx->n);
+    SG_CUDA(cudaMemcpy(ctx->ptype.ptr, particle_type, ctx->n * sizeof(int), cudaMemcpyHostToDevice));
+    ctx->n_types = n_types;
+    ctx->t_diag = diagonal ? 1 : 0;
+    ctx->t_ready = true;
+    return SG_OK;
+  });
+}
+
+// reference-layout device vector -> padded device vector (returns the padded pointer)
+static const double2 *to_padded(sg_context *c, const double2 *src, sg::DevBuf<double2> &pad, int R, cudaStream_t st) {
+  if (c->uniform) return src;
+  pad.reserve(c->padded(R));
+  sg::k_zero(pad.ptr, c->padded(R), st);
+  sg::k_gather(src, pad.ptr, c->map.ptr, c->n_unknowns, R, st);
+  c->launches += 2;
+  return pad.ptr;
+}
+
+static void matvec_dev(sg_context *c, const double2 *x, double2 *y, int R, int precision, bool master,
+                       cudaStream_t st) {
+  require_ready(c, master);
+  SG_REQUIRE(R >= 1 && R <= 256, "nrhs must be in [1, 256]");
+  SG_REQUIRE(precision == SG_FP64 || precision == SG_FP32, "unknown precision");
+  use_device(c);
+  const bool fp32 = precision == SG_FP32;
+  if (fp32) ensure_pairs(c, st);
+  const double2 *xp = to_padded(c, x, c->pad_in, R, st);
+  double2 *yp = y;
+  if (!c->uniform) {
+    c->pad_out.reserve(c->padded(R));
+    yp = c->pad_out.ptr;
+  }
+  sg::apply_padded(c, xp, yp, R, master, fp32, st);
+  if (!c->uniform) {
+    sg::k_scatter(yp, y, c->map.ptr, c->n_unknowns, R, st);
+    c->launches += 1;
+  }
+}
+
+static int matvec_host(sg_context *ctx, const double *x, double *y, int nrhs, int precision, bool master) {
+  return guarded([&]() -> int {
+    require_ready(ctx, master);
+    SG_REQUIRE(x && y, "null vector");
+    SG_REQUIRE(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
+    const size_t len = (size_t)ctx->n_unknowns * nrhs;
+    if (!all_finite(x, 2 * len)) throw sg::Error{SG_ERR_NAN, "input vector holds NaN or Inf"};
+    use_device(ctx);
+    cudaStream_t st = ctx->stream;
+    ctx->io_in.reserve(len);
+    ctx->io_out.reserve(len);
+    SG_CUDA(cudaMemcpyAsync(ctx->io_in.ptr, x, len * sizeof(double2), cudaMemcpyHostToDevice, st));
+    matvec_dev(ctx, ctx->io_in.ptr, ctx->io_out.ptr, nrhs, precision, master, st);
+    SG_CUDA(cudaMemcpyAsync(y, ctx->io_out.ptr, len * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    SG_CUDA(cudaStreamSynchronize(st));
+    return SG_OK;
+  });
+}
+
+int sg_coupling_matvec(sg_context *ctx, const double *x, double *y, int nrhs, int precision) {
+  return matvec_host(ctx, x, y, nrhs, precision, false);
+}
+
+int sg_master_matvec(sg_context *ctx, const double *x, double *y, int nrhs, int precision) {
+  return matvec_host(ctx, x, y, nrhs, precision, true);
+}
+
+int sg_coupling_matvec_dev(sg_context *ctx, const void *x, void *y, int nrhs, int precision, void *stream) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(x && y, "null vector");
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    matvec_dev(ctx, (const double2 *)x, (double2 *)y, nrhs, precision, false, st);
+    return SG_OK;
+  });
+}
+
+int sg_master_matvec_dev(sg_context *ctx, const void *x, void *y, int nrhs, int precision, void *stream) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(x && y, "null vector");
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    matvec_dev(ctx, (const double2 *)x, (double2 *)y, nrhs, precision, true, st);
+    return SG_OK;
+  });
+}
+
+static int solve_dev_impl(sg_context *ctx, const double2 *b, double2 *x, int nrhs, double rtol, int restart,
+                          int maxiter, int precision, sg_solve_info *info, cudaStream_t st) {
+  require_ready(ctx, true);
+  SG_REQUIRE(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
+  SG_REQUIRE(rtol > 0 && std::isfinite(rtol), "rtol must be positive");
+  SG_REQUIRE(restart >= 0 && restart <= 64, "restart must be in [0, 64] (0 = 20)");
+  SG_REQUIRE(precision == SG_FP64 || precision == SG_FP32, "unknown precision");
+  use_device(ctx);
+  if (precision == SG_FP32) ensure_pairs(ctx, st);
+  const size_t plen = ctx->padded(nrhs);
+  const double2 *bp = b;
+  double2 *xp = x;
+  if (!ctx->uniform) {
+    ctx->sol_b.reserve(plen);
+    ctx->sol_x.reserve(plen);
+    sg::k_zero(ctx->sol_b.ptr, plen, st);
+    sg::k_zero(ctx->sol_x.ptr, plen, st);
+    sg::k_gather(b, ctx->sol_b.ptr, ctx->map.ptr, ctx->n_unknowns, nrhs, st);
+    sg::k_gather(x, ctx->sol_x.ptr, ctx->map.ptr, ctx->n_unknowns, nrhs, st);
+    ctx->launches += 4;
+    bp = ctx->sol_b.ptr;
+    xp = ctx->sol_x.ptr;
+  }
+  sg_solve_info local{};
+  sg::solve_padded(ctx, bp, xp, nrhs, rtol, restart, maxiter, precision, &local, st);
+  if (!ctx->uniform) {
+    sg::k_scatter(xp, x, ctx->map.ptr, ctx->n_unknowns, nrhs, st);
+    ctx->launches += 1;
+  }
+  if (info) *info = local;
+  if (!std::isfinite(local.max_rel_residual)) throw sg::Error{SG_ERR_NAN, "solver produced NaN or Inf"};
+  if (local.converged < nrhs) {
+    sg::set_error("GMRES did not reach the tolerance for every right-hand side");
+    return SG_ERR_NOT_CONVERGED;
+  }
+  return SG_OK;
+}
+
+int sg_gmres_solve(sg_context *ctx, const double *b, double *x, int nrhs, double rtol, int restart, int maxiter,
+                   int precision, sg_solve_info *info) {
+  return guarded([&]() -> int {
+    require_ready(ctx, true);
+    SG_REQUIRE(b && x, "null vector");
+    SG_REQUIRE(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
+    const size_t len = (size_t)ctx->n_unknowns * nrhs;
+    if (!all_finite(b, 2 * len) || !all_finite(x, 2 * len))
+      throw sg::Error{SG_ERR_NAN, "right-hand side or initial guess holds NaN or Inf"};
+    use_device(ctx);
+    cudaStream_t st = ctx->stream;
+    ctx->io_in.reserve(len);
+    ctx->io_out.reserve(len);
+    SG_CUDA(cudaMemcpyAsync(ctx->io_in.ptr, b, len * sizeof(double2), cudaMemcpyHostToDevice, st));
+    SG_CUDA(cudaMemcpyAsync(ctx->io_out.ptr, x, len * sizeof(double2), cudaMemcpyHostToDevice, st));
+    int rc = solve_dev_impl(ctx, ctx->io_in.ptr, ctx->io_out.ptr, nrhs, rtol, restart, maxiter, precision, info, st);
+    SG_CUDA(cudaMemcpyAsync(x, ctx->io_out.ptr, len * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    SG_CUDA(cudaStreamSynchronize(st));
+    return rc;
+  });
+}
+
+int sg_gmres_solve_dev(sg_context *ctx, const void *b, void *x, int nrhs, double rtol, int restart, int maxiter,
+                       int precision, sg_solve_info *info, void *stream) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(b && x, "null vector");
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    return solve_dev_impl(ctx, (const double2 *)b, (double2 *)x, nrhs, rtol, restart, maxiter, precision, info, st);
+  });
+}
+
+int sg_true_residual(sg_context *ctx, const double *b, const double *x, int nrhs, double *rel_residual) {
+  return guarded([&]() -> int {
+    require_ready(ctx, true);
+    SG_REQUIRE(b && x && rel_residual, "null argument");
+    SG_REQUIRE(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
+    const size_t len = (size_t)ctx->n_unknowns * nrhs;
+    use_device(ctx);
+    cudaStream_t st = ctx->stream;
+    ctx->io_in.reserve(len);
+    ctx->io_out.reserve(len);
+    SG_CUDA(cudaMemcpyAsync(ctx->io_in.ptr, b, len * sizeof(double2), cudaMemcpyHostToDevice, st));
+    SG_CUDA(cudaMemcpyAsync(ctx->io_out.ptr, x, len * sizeof(double2), cudaMemcpyHostToDevice, st));
+    const double2 *bp = to_padded(ctx, ctx->io_in.ptr, ctx->sol_b, nrhs, st);
+    const double2 *xp = to_padded(ctx, ctx->io_out.ptr, ctx->sol_x, nrhs, st);
+    sg::residual_norms(ctx, bp, xp, nrhs, rel_residual, st);
+    return SG_OK;
+  });
+}
+
+int sg_profile(sg_context *ctx, int enable) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx != nullptr, "null context");
+    ctx->profiling = enable != 0;
+    return SG_OK;
+  });
+}
+
+int sg_kernel_timing(sg_context *ctx, double *total_ms, int64_t *count, int reset) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx != nullptr, "null context");
+    use_device(ctx);
+    for (auto &ev : ctx->events) {
+      SG_CUDA(cudaEventSynchronize(ev.second));
+      float ms = 0.f;
+      SG_CUDA(cudaEventElapsedTime(&ms, ev.first, ev.second));
+      ctx->coupling_ms += ms;
+      ctx->coupling_launches += 1;
+      cudaEventDestroy(ev.first);
+      cudaEventDestroy(ev.second);
+    }
+    ctx->events.clear();
+    if (total_ms) *total_ms = ctx->coupling_ms;
+    if (count) *count = ctx->coupling_launches;
+    if (reset) {
+      ctx->coupling_ms = 0.0;
+      ctx->coupling_launches = 0;
+    }
+    return SG_OK;
+  });
+}
+
+int sg_launch_count(sg_context *ctx, int64_t *count) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx && count, "null argument");
+    *count = ctx->launches;
+    return SG_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,618 @@
+// GMRES(m) on the master operator M = 1 - T W, on the device.
+//
+// Mirrors the control flow of scipy.sparse.linalg.gmres as called by the reference
+// (smuthi/linearsystem/linear_system.py:285): x0 = given, restart m, stop when
+// ||b - M x|| <= rtol ||b||, Givens-rotated Hessenberg least squares, adaptive inner
+// tolerance, explicit residual at every restart. Differences: orthogonalisation is
+// classical Gram-Schmidt applied twice (CGS2; as stable as scipy's MGS and four
+// batched kernels instead of 2(j+1) dependent ones), and nrhs > 1 right-hand sides
+// run independent Krylov spaces in lockstep that share one block matvec per step.
+//
+// Vectors live in the padded layout [particle][blocksize][nrhs] (double2).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <vector>
+
+#include "sg_internal.h"
+
+namespace sg {
+
+typedef std::complex<double> cd;
+static constexpr int kMaxVec = 66;  // restart <= 64, plus w and one spare
+static constexpr int kHcol = 2 * kMaxVec + 4;  // per-rhs slots of the Arnoldi scalar buffer
+
+struct VecList {
+  const double2 *v[kMaxVec];
+};
+
+// partial[blk][k][r] = sum_{rows in blk} conj(V_k[row][r]) * w[row][r]
+__global__ void dots_partial_kernel(VecList V, int nvec, const double2 *w, size_t rows, int R, double2 *partial) {
+  extern __shared__ double2 sd[];
+  const int tpr = blockDim.x / R;  // threads per rhs column (blockDim.x is a multiple of R)
+  const int r = threadIdx.x % R, lr = threadIdx.x / R;
+  const size_t nblk = gridDim.x;
+  for (int k = 0; k < nvec; ++k) {
+    double sr = 0.0, si = 0.0;
+    for (size_t row = blockIdx.x * (size_t)tpr + lr; row < rows; row += nblk * tpr) {
+      const double2 a = V.v[k][row * R + r], b = w[row * R + r];
+      sr = fma(a.x, b.x, fma(a.y, b.y, sr));
+      si = fma(a.x, b.y, fma(-a.y, b.x, si));
+    }
+    sd[threadIdx.x] = make_double2(sr, si);
+    __syncthreads();
+    // reduce over lr for each r (tree over the lr index)
+    for (int s = tpr / 2; s > 0; s >>= 1) {
+      if (lr < s) {
+        const double2 o = sd[threadIdx.x + s * R];
+        sd[threadIdx.x].x += o.x;
+        sd[threadIdx.x].y += o.y;
+      }
+      __syncthreads();
+    }
+    if (lr == 0) partial[((size_t)blockIdx.x * nvec + k) * R + r] = sd[r];
+    __syncthreads();
+  }
+}
+
+__global__ void dots_final_kernel(const double2 *partial, int nblk, int nvec, int R, double2 *out) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nvec * R) return;
+  double sr = 0.0, si = 0.0;
+  for (int b = 0; b < nblk; ++b) {
+    const double2 v = partial[(size_t)b * nvec * R + e];
+    sr += v.x;
+    si += v.y;
+  }
+  out[e] = make_double2(sr, si);
+}
+
+// y[row][r] += sign * sum_k V_k[row][r] * c[k][r]
+__global__ void combine_kernel(VecList V, int nvec, const double2 *c, double sign, double2 *y, size_t rows, int R) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= rows * R) return;
+  const int r = (int)(e % R);
+  double2 acc = y[e];
+  for (int k = 0; k < nvec; ++k) {
+    const double2 a = V.v[k][e], h = c[k * R + r];
+    acc.x = fma(sign * a.x, h.x, fma(-sign * a.y, h.y, acc.x));
+    acc.y = fma(sign * a.x, h.y, fma(sign * a.y, h.x, acc.y));
+  }
+  y[e] = acc;
+}
+
+// y = x * s[r] (real scale per rhs)
+__global__ void scale_kernel(const double2 *x, const double *s, double2 *y, size_t rows, int R) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= rows * R) return;
+  const double f = s[e % R];
+  y[e] = make_double2(x[e].x * f, x[e].y * f);
+}
+
+// r = b - r (residual from a master-matvec result)
+__global__ void sub_from_kernel(const double2 *b, double2 *r, size_t n) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  r[e] = make_double2(b[e].x - r[e].x, b[e].y - r[e].y);
+}
+
+// x += d * mask[r]
+__global__ void add_masked_kernel(double2 *x, const double2 *d, const double *mask, size_t rows, int R) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= rows * R) return;
+  const double f = mask[e % R];
+  x[e].x += f * d[e].x;
+  x[e].y += f * d[e].y;
+}
+
+__global__ void zero_kernel(double2 *p, size_t n) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) p[e] = make_double2(0.0, 0.0);
+}
+
+__global__ void gather_kernel(const double2 *src, double2 *dst, const int *map, int nu, int R) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)nu * R) return;
+  const int u = (int)(e / R), r = (int)(e % R);
+  dst[(size_t)map[u] * R + r] = src[e];
+}
+
+__global__ void scatter_kernel(const double2 *src, double2 *dst, const int *map, int nu, int R) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)nu * R) return;
+  const int u = (int)(e / R), r = (int)(e % R);
+  dst[e] = src[(size_t)map[u] * R + r];
+}
+
+static inline unsigned nblocks(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+void k_zero(double2 *p, size_t n, cudaStream_t st) {
+  if (!n) return;
+  zero_kernel<<<nblocks(n), 256, 0, st>>>(p, n);
+  SG_CUDA(cudaGetLastError());
+}
+void k_gather(const double2 *src, double2 *dst, const int *map, int nu, int R, cudaStream_t st) {
+  gather_kernel<<<nblocks((size_t)nu * R), 256, 0, st>>>(src, dst, map, nu, R);
+  SG_CUDA(cudaGetLastError());
+}
+void k_scatter(const double2 *src, double2 *dst, const int *map, int nu, int R, cudaStream_t st) {
+  scatter_kernel<<<nblocks((size_t)nu * R), 256, 0, st>>>(src, dst, map, nu, R);
+  SG_CUDA(cudaGetLastError());
+}
+
+// ------------------------------------------------------------------ operator + dots
+void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool master, bool fp32, cudaStream_t st);
+
+struct Solver {
+  sg_context *c;
+  cudaStream_t st;
+  int R;
+  size_t rows;  // padded rows = n * bs
+  int64_t *launches;
+
+  size_t len() const { return rows * R; }
+
+  // y = M x on padded vectors with the FP64 or FP32 operator
+  void master(const double2 *x, double2 *y, bool fp32) { apply_padded(c, x, y, R, true, fp32, st); }
+
+  // out[k][r] = <V_k, w> for k < nvec (device), copied to host h (nvec * R)
+  void dots(const VecList &V, int nvec, const double2 *w, double2 *dout) {
+    int tpb = 256;
+    const int tpr = std::max(1, tpb / R);
+    int p2 = 1;
+    while (p2 * 2 <= tpr) p2 *= 2;
+    tpb = p2 * R;
+    const int nblk = (int)std::min<size_t>(152 * 2, (rows + p2 - 1) / p2);
+    c->w_tmp.reserve((size_t)nblk * nvec * R);
+    dots_partial_kernel<<<nblk, tpb, tpb * sizeof(double2), st>>>(V, nvec, w, rows, R, c->w_tmp.ptr);
+    SG_CUDA(cudaGetLastError());
+    dots_final_kernel<<<nblocks((size_t)nvec * R), 256, 0, st>>>(c->w_tmp.ptr, nblk, nvec, R, dout);
+    SG_CUDA(cudaGetLastError());
+    *launches += 2;
+  }
+
+  void combine(const VecList &V, int nvec, const double2 *coef, double sign, double2 *y) {
+    combine_kernel<<<nblocks(len()), 256, 0, st>>>(V, nvec, coef, sign, y, rows, R);
+    SG_CUDA(cudaGetLastError());
+    *launches += 1;
+  }
+};
+
+// LAPACK zlartg convention: [c s; -conj(s) c] [f; g] = [r; 0], c real.
+static void lartg(cd f, cd g, double &cs, cd &sn, cd &r) {
+  const double af = std::abs(f), ag = std::abs(g);
+  if (ag == 0.0) {
+    cs = 1.0;
+    sn = 0.0;
+    r = f;
+    return;
+  }
+  if (af == 0.0) {
+    cs = 0.0;
+    sn = std::conj(g) / ag;
+    r = ag;
+    return;
+  }
+  const double nrm = std::hypot(af, ag);
+  cs = af / nrm;
+  const cd fs = f / af;
+  sn = fs * std::conj(g) / nrm;
+  r = fs * nrm;
+}
+
+struct GmresResult {
+  int inner_iters = 0;
+  int cycles = 0;
+  int matvecs = 0;
+  std::vector<double> relres;  // per rhs: final ||b - M x|| / ||b|| with the solve's operator
+  std::vector<char> conv;
+};
+
+// Lockstep GMRES on padded device vectors. b, x: len(); x holds x0 (zero_x0 = x0 is zero).
+static GmresResult gmres_lockstep(Solver &S, const double2 *b, double2 *x, double rtol, int restart, int maxiter,
+                                  bool fp32, bool zero_x0, const std::vector<char> &skip) {
+  sg_context *c = S.c;
+  const int R = S.R;
+  const size_t len = S.len();
+  restart = std::max(1, std::min(restart, (int)std::min<size_t>(S.rows, 64)));
+  c->w_basis.reserve((size_t)(restart + 1) * len);
+  c->w_w.reserve(len);
+  c->w_r.reserve(len);
+  c->w_hcol.reserve((size_t)kHcol * R);
+  c->w_red.reserve((size_t)4 * R + 4);
+  double2 *V0 = c->w_basis.ptr;
+  double2 *w = c->w_w.ptr;
+  double2 *r = c->w_r.ptr;
+  double2 *dh = c->w_hcol.ptr;
+  auto Vk = [&](int k) { return V0 + (size_t)k * len; };
+  const double eps = 2.220446049250313e-16;
+  GmresResult res;
+  res.relres.assign(R, 0.0);
+  res.conv.assign(R, 0);
+
+  // ||b||
+  std::vector<double2> hb((size_t)kHcol * R);
+  VecList L1{};
+  L1.v[0] = b;
+  S.dots(L1, 1, b, dh);
+  SG_CUDA(cudaMemcpyAsync(hb.data(), dh, R * sizeof(double2), cudaMemcpyDeviceToHost, S.st));
+  SG_CUDA(cudaStreamSynchronize(S.st));
+  std::vector<double> bnrm(R), atol(R), ptol(R), pfac(R, 1.0), presid(R, 0.0), rnorm(R, 0.0);
+  std::vector<char> active(R, 1);
+  for (int q = 0; q < R; ++q) {
+    bnrm[q] = std::sqrt(std::max(0.0, hb[q].x));
+    atol[q] = rtol * bnrm[q];
+    if (bnrm[q] == 0.0 || (!skip.empty() && skip[q])) {
+      active[q] = 0;
+      res.conv[q] = 1;
+    }
+  }
+  // r = b - M x0
+  if (zero_x0) {
+    SG_CUDA(cudaMemcpyAsync(r, b, len * sizeof(double2), cudaMemcpyDeviceToDevice, S.st));
+  } else {
+    S.master(x, r, fp32);
+    res.matvecs++;
+    sub_from_kernel<<<nblocks(len), 256, 0, S.st>>>(b, r, len);
+    SG_CUDA(cudaGetLastError());
+    // already converged at x0?
+    L1.v[0] = r;
+    S.dots(L1, 1, r, dh);
+    SG_CUDA(cudaMemcpyAsync(hb.data(), dh, R * sizeof(double2), cudaMemcpyDeviceToHost, S.st));
+    SG_CUDA(cudaStreamSynchronize(S.st));
+    for (int q = 0; q < R; ++q) {
+      rnorm[q] = std::sqrt(std::max(0.0, hb[q].x));
+      if (active[q] && rnorm[q] < atol[q]) {
+        active[q] = 0;
+        res.conv[q] = 1;
+      }
+    }
+  }
+  for (int q = 0; q < R; ++q) ptol[q] = bnrm[q] * std::min(1.0, bnrm[q] > 0 ? atol[q] / bnrm[q] : 1.0);
+
+  std::vector<cd> H((size_t)restart * (restart + 1) * R), G((size_t)restart * R), Sv((size_t)(restart + 1) * R);
+  std::vector<double> Gc((size_t)restart * R);
+  std::vector<double> hscale(R), hmask(R);
+  std::vector<int> colstop(R);
+  std::vector<char> inner_done(R), breakdown(R);
+  int inner_iter = 0;
+  c->w_d.reserve(len);
+
+  for (int cycle = 0; cycle < maxiter; ++cycle) {
+    bool any = false;
+    for (int q = 0; q < R; ++q) any |= active[q] != 0;
+    if (!any) break;
+    res.cycles++;
+    // v0 = r / ||r||
+    L1.v[0] = r;
+    S.dots(L1, 1, r, dh);
+    SG_CUDA(cudaMemcpyAsync(hb.data(), dh, R * sizeof(double2), cudaMemcpyDeviceToHost, S.st));
+    SG_CUDA(cudaStreamSynchronize(S.st));
+    for (int q = 0; q < R; ++q) {
+      const double nr = std::sqrt(std::max(0.0, hb[q].x));
+      hscale[q] = nr > 0 ? 1.0 / nr : 0.0;
+      for (int k = 0; k <= restart; ++k) Sv[(size_t)k * R + q] = 0.0;
+      Sv[q] = nr;
+      inner_done[q] = active[q] ? 0 : 1;
+      breakdown[q] = 0;
+      colstop[q] = -1;
+      if (active[q] && nr == 0.0) inner_done[q] = 1;
+    }
+    double *dscale = c->w_red.ptr;
+    SG_CUDA(cudaMemcpyAsync(dscale, hscale.data(), R * sizeof(double), cudaMemcpyHostToDevice, S.st));
+    scale_kernel<<<nblocks(len), 256, 0, S.st>>>(r, dscale, Vk(0), S.rows, R);
+    SG_CUDA(cudaGetLastError());
+
+    int col = 0;
+    for (col = 0; col < restart; ++col) {
+      bool all_done = true;
+      for (int q = 0; q < R; ++q) all_done &= inner_done[q] != 0;
+      if (all_done) break;
+      // w = M v_col
+      S.master(Vk(col), w, fp32);
+      res.matvecs++;
+      // pass 1: dots with V_0..V_col and w itself (h0^2)
+      VecList L{};
+      for (int k = 0; k <= col; ++k) L.v[k] = Vk(k);
+      L.v[col + 1] = w;
+      S.dots(L, col + 2, w, dh);
+      S.combine(L, col + 1, dh, -1.0, w);
+      // pass 2: re-orthogonalise, then ||w||^2
+      double2 *dh2 = dh + (size_t)(col + 2) * R;
+      S.dots(L, col + 1, w, dh2);
+      S.combine(L, col + 1, dh2, -1.0, w);
+      double2 *dn = dh2 + (size_t)(col + 1) * R;
+      L1.v[0] = w;
+      S.dots(L1, 1, w, dn);
+      const size_t nh = (size_t)(2 * col + 4) * R;
+      SG_CUDA(cudaMemcpyAsync(hb.data(), dh, nh * sizeof(double2), cudaMemcpyDeviceToHost, S.st));
+      SG_CUDA(cudaStreamSynchronize(S.st));
+      inner_iter++;
+      for (int q = 0; q < R; ++q) {
+        cd *h = &H[((size_t)q * restart + col) * (restart + 1)];
+        const double h0 = std::sqrt(std::max(0.0, hb[(size_t)(col + 1) * R + q].x));
+        for (int k = 0; k <= col; ++k) {
+          const double2 a = hb[(size_t)k * R + q], a2 = hb[(size_t)(col + 2 + k) * R + q];
+          h[k] = cd(a.x + a2.x, a.y + a2.y);
+        }
+        const double h1 = std::sqrt(std::max(0.0, hb[(size_t)(2 * col + 3) * R + q].x));
+        h[col + 1] = h1;
+        hscale[q] = (h1 > 0) ? 1.0 / h1 : 0.0;
+        if (inner_done[q]) continue;
+        bool bd = false;
+        if (h1 <= eps * h0) {
+          h[col + 1] = 0.0;
+          bd = true;
+        }
+        // apply previous rotations
+        for (int k = 0; k < col; ++k) {
+          const double cs = Gc[(size_t)q * restart + k];
+          const cd sn = G[(size_t)q * restart + k];
+          const cd n0 = h[k], n1 = h[k + 1];
+          h[k] = cs * n0 + sn * n1;
+          h[k + 1] = -std::conj(sn) * n0 + cs * n1;
+        }
+        double cs;
+        cd sn, rr;
+        lartg(h[col], h[col + 1], cs, sn, rr);
+        Gc[(size_t)q * restart + col] = cs;
+        G[(size_t)q * restart + col] = sn;
+        h[col] = rr;
+        h[col + 1] = 0.0;
+        const cd tmp = -std::conj(sn) * Sv[(size_t)col * R + q];
+        Sv[(size_t)col * R + q] = cs * Sv[(size_t)col * R + q];
+        Sv[(size_t)(col + 1) * R + q] = tmp;
+        presid[q] = std::abs(tmp);
+        colstop[q] = col;
+        if (presid[q] <= ptol[q] || bd) {
+          inner_done[q] = 1;
+          breakdown[q] = bd;
+        }
+      }
+      // v_{col+1} = w / h1
+      SG_CUDA(cudaMemcpyAsync(dscale, hscale.data(), R * sizeof(double), cudaMemcpyHostToDevice, S.st));
+      scale_kernel<<<nblocks(len), 256, 0, S.st>>>(w, dscale, Vk(col + 1), S.rows, R);
+      SG_CUDA(cudaGetLastError());
+    }
+    // y = H^{-1} S per rhs; x += V y
+    std::vector<double2> ycoef((size_t)(restart + 1) * R, make_double2(0, 0));
+    int maxcol = -1;
+    for (int q = 0; q < R; ++q) {
+      if (!active[q] || colstop[q] < 0) continue;
+      const int cq = colstop[q];
+      maxcol = std::max(maxcol, cq);
+      auto hq = [&](int cc, int k) -> cd & { return H[((size_t)q * restart + cc) * (restart + 1) + k]; };
+      std::vector<cd> y(cq + 1);
+      if (hq(cq, cq) == 0.0) Sv[(size_t)cq * R + q] = 0.0;
+      for (int k = 0; k <= cq; ++k) y[k] = Sv[(size_t)k * R + q];
+      for (int k = cq; k > 0; --k) {
+        if (y[k] != 0.0) {
+          y[k] /= hq(k, k);
+          const cd t = y[k];
+          for (int a = 0; a < k; ++a) y[a] -= t * hq(k, a);
+        }
+      }
+      if (y[0] != 0.0) y[0] /= hq(0, 0);
+      for (int k = 0; k <= cq; ++k) ycoef[(size_t)k * R + q] = make_double2(y[k].real(), y[k].imag());
+    }
+    if (maxcol >= 0) {
+      SG_CUDA(cudaMemcpyAsync(dh, ycoef.data(), (size_t)(maxcol + 1) * R * sizeof(double2), cudaMemcpyHostToDevice,
+                              S.st));
+      VecList L{};
+      for (int k = 0; k <= maxcol; ++k) L.v[k] = Vk(k);
+      S.combine(L, maxcol + 1, dh, 1.0, x);
+    }
+    // explicit residual r = b - M x
+    S.master(x, r, fp32);
+    res.matvecs++;
+    sub_from_kernel<<<nblocks(len), 256, 0, S.st>>>(b, r, len);
+    SG_CUDA(cudaGetLastError());
+    L1.v[0] = r;
+    S.dots(L1, 1, r, dh);
+    SG_CUDA(cudaMemcpyAsync(hb.data(), dh, R * sizeof(double2), cudaMemcpyDeviceToHost, S.st));
+    SG_CUDA(cudaStreamSynchronize(S.st));
+    for (int q = 0; q < R; ++q) {
+      rnorm[q] = std::sqrt(std::max(0.0, hb[q].x));
+      if (!active[q]) continue;
+      if (rnorm[q] <= atol[q]) {
+        active[q] = 0;
+        res.conv[q] = 1;
+        continue;
+      }
+      if (breakdown[q]) {
+        active[q] = 0;
+        continue;
+      }
+      if (presid[q] <= ptol[q]) pfac[q] = std::max(eps, 0.25 * pfac[q]);
+      else pfac[q] = std::min(1.0, 1.5 * pfac[q]);
+      ptol[q] = presid[q] * std::min(pfac[q], atol[q] / rnorm[q]);
+    }
+  }
+  res.inner_iters = inner_iter;
+  for (int q = 0; q < R; ++q) {
+    if (bnrm[q] > 0) res.relres[q] = rnorm[q] / bnrm[q];
+    if (bnrm[q] == 0.0) res.conv[q] = 1;
+  }
+  return res;
+}
+
+// Mixed precision: FP32-operator GMRES corrections inside FP64 iterative refinement.
+static GmresResult refine_mixed(Solver &S, const double2 *b, double2 *x, double rtol, int restart, int maxiter,
+                                int &fp64_mv, int &fp32_mv, int &steps) {
+  sg_context *c = S.c;
+  const int R = S.R;
+  const size_t len = S.len();
+  c->w_b.reserve(len);  // residual (rhs of the correction solve)
+  c->w_x.reserve(len);  // correction
+  double2 *rr = c->w_b.ptr, *d = c->w_x.ptr;
+  std::vector<double2> hb(2 * R);
+  GmresResult out;
+  out.relres.assign(R, 0.0);
+  out.conv.assign(R, 0);
+  c->w_hcol.reserve((size_t)kHcol * R);
+  c->w_red.reserve((size_t)4 * R + 4);
+  double2 *dh = c->w_hcol.ptr;
+  VecList L1{};
+  L1.v[0] = b;
+  S.dots(L1, 1, b, dh);
+  SG_CUDA(cudaMemcpyAsync(hb.data(), dh, R * sizeof(double2), cudaMemcpyDeviceToHost, S.st));
+  SG_CUDA(cudaStreamSynchronize(S.st));
+  std::vector<double> bnrm(R);
+  for (int q = 0; q < R; ++q) bnrm[q] = std::sqrt(std::max(0.0, hb[q].x));
+  std::vector<char> done(R, 0);
+  std::vector<double> mask(R);
+  const int max_steps = 40;
+  int inner_total = 0;
+  for (steps = 0; steps <= max_steps; ++steps) {
+    // FP64 true residual
+    S.master(x, rr, false);
+    fp64_mv++;
+    sub_from_kernel<<<nblocks(len), 256, 0, S.st>>>(b, rr, len);
+    SG_CUDA(cudaGetLastError());
+    L1.v[0] = rr;
+    S.dots(L1, 1, rr, dh);
+    SG_CUDA(cudaMemcpyAsync(hb.data(), dh, R * sizeof(double2), cudaMemcpyDeviceToHost, S.st));
+    SG_CUDA(cudaStreamSynchronize(S.st));
+    double worst = 0.0;
+    std::vector<double> rn(R);
+    for (int q = 0; q < R; ++q) {
+      rn[q] = std::sqrt(std::max(0.0, hb[q].x));
+      const double rel = bnrm[q] > 0 ? rn[q] / bnrm[q] : 0.0;
+      out.relres[q] = rel;
+      done[q] = rel <= rtol ? 1 : 0;
+      out.conv[q] = done[q];
+      if (!done[q]) worst = std::max(worst, rel);
+    }
+    if (worst == 0.0 || steps == max_steps || inner_total >= maxiter) break;
+    // correction solve with the FP32 operator: tolerance relative to the current residual
+    double tau = 0.3 * rtol / worst;
+    tau = std::max(1e-6, std::min(0.5, tau));
+    k_zero(d, len, S.st);
+    GmresResult g = gmres_lockstep(S, rr, d, tau, restart, std::max(1, (maxiter - inner_total) / restart + 1), true,
+                                   true, done);
+    fp32_mv += g.matvecs;
+    inner_total += g.inner_iters;
+    out.inner_iters += g.inner_iters;
+    out.cycles += g.cycles;
+    for (int q = 0; q < R; ++q) mask[q] = done[q] ? 0.0 : 1.0;
+    dh = c->w_hcol.ptr;
+    double *dm = c->w_red.ptr;
+    SG_CUDA(cudaMemcpyAsync(dm, mask.data(), R * sizeof(double), cudaMemcpyHostToDevice, S.st));
+    add_masked_kernel<<<nblocks(len), 256, 0, S.st>>>(x, d, dm, S.rows, R);
+    SG_CUDA(cudaGetLastError());
+  }
+  return out;
+}
+
+// Public driver used by the C ABI: padded device vectors b, x (x holds x0).
+void solve_padded(sg_context *c, const double2 *b, double2 *x, int R, double rtol, int restart, int maxiter,
+                  int precision, sg_solve_info *info, cudaStream_t st) {
+  Solver S{c, st, R, (size_t)c->n * c->bs, &c->launches};
+  if (maxiter <= 0) maxiter = 10 * c->n_unknowns;
+  if (restart <= 0) restart = 20;
+  const auto t0 = std::chrono::steady_clock::now();
+  GmresResult g;
+  int fp64_mv = 0, fp32_mv = 0, steps = 0;
+  if (precision == SG_FP32) {
+    g = refine_mixed(S, b, x, rtol, restart, maxiter * restart, fp64_mv, fp32_mv, steps);
+  } else {
+    g = gmres_lockstep(S, b, x, rtol, restart, maxiter, false, false, std::vector<char>());
+    fp64_mv = g.matvecs;
+    steps = g.cycles;
+  }
+  SG_CUDA(cudaStreamSynchronize(st));
+  const auto t1 = std::chrono::steady_clock::now();
+  if (info) {
+    info->iterations = g.inner_iters;
+    info->restarts = steps;
+    info->fp64_matvecs = fp64_mv;
+    info->fp32_matvecs = fp32_mv;
+    int nc = 0;
+    double mx = 0.0;
+    for (int q = 0; q < R; ++q) {
+      nc += g.conv[q] ? 1 : 0;
+      mx = std::max(mx, g.relres[q]);
+    }
+    info->converged = nc;
+    info->reserved = 0;
+    info->max_rel_residual = mx;
+    info->seconds = std::chrono::duration<double>(t1 - t0).count();
+  }
+}
+
+// y = M x or W x on padded vectors (public matvec entry points)
+void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool master, bool fp32, cudaStream_t st) {
+  CouplingLaunch L{};
+  L.pos = c->pos.ptr;
+  L.mofn = c->mofn.ptr;
+  L.coef = fp32 ? (const void *)c->coef32.ptr : (const void *)c->coef64.ptr;
+  L.pairs = fp32 ? c->pairs.ptr : nullptr;
+  L.n = c->n;
+  L.bs = c->bs;
+  L.n_int = c->n_int;
+  L.ncoef = c->ncoef;
+  L.rho_min = c->rho_min;
+  L.res = c->res;
+  L.x = x;
+  L.y = y;
+  L.nrhs = R;
+  L.master = master ? 1 : 0;
+  L.t = c->tmat.ptr;
+  L.ptype = c->ptype.ptr;
+  L.t_diag = c->t_diag;
+  const int ns = choose_split(c->n, R);
+  if (ns > 1) {
+    c->w_partial.reserve((size_t)ns * c->n * c->bs * R);
+    L.partial = c->w_partial.ptr;
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (c->profiling) {
+    SG_CUDA(cudaEventCreate(&e0));
+    SG_CUDA(cudaEventCreate(&e1));
+    SG_CUDA(cudaEventRecord(e0, st));
+  }
+  c->launches += launch_coupling(L, fp32, ns, st);
+  if (c->profiling) {
+    SG_CUDA(cudaEventRecord(e1, st));
+    c->events.push_back({e0, e1});
+  }
+}
+
+}  // namespace sg
+
+namespace sg {
+
+__global__ void residual_kernel_sub(const double2 *b, double2 *r, size_t n) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) r[e] = make_double2(b[e].x - r[e].x, b[e].y - r[e].y);
+}
+
+// rel[q] = ||b_q - M x_q|| / ||b_q|| with the FP64 operator (padded device vectors)
+void residual_norms(sg_context *c, const double2 *b, const double2 *x, int R, double *rel, cudaStream_t st) {
+  Solver S{c, st, R, (size_t)c->n * c->bs, &c->launches};
+  const size_t len = S.len();
+  c->w_r.reserve(len);
+  c->w_hcol.reserve((size_t)kHcol * R);
+  S.master(x, c->w_r.ptr, false);
+  residual_kernel_sub<<<nblocks(len), 256, 0, st>>>(b, c->w_r.ptr, len);
+  SG_CUDA(cudaGetLastError());
+  VecList L{};
+  L.v[0] = b;
+  L.v[1] = c->w_r.ptr;
+  S.dots(L, 1, b, c->w_hcol.ptr);
+  VecList L2{};
+  L2.v[0] = c->w_r.ptr;
+  S.dots(L2, 1, c->w_r.ptr, c->w_hcol.ptr + R);
+  std::vector<double2> h(2 * R);
+  SG_CUDA(cudaMemcpyAsync(h.data(), c->w_hcol.ptr, 2 * R * sizeof(double2), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(cudaStreamSynchronize(st));
+  for (int q = 0; q < R; ++q) {
+    const double bn = std::sqrt(std::max(0.0, h[q].x)), rn = std::sqrt(std::max(0.0, h[R + q].x));
+    rel[q] = bn > 0 ? rn / bn : rn;
+  }
+}
+
+}  // namespace sg

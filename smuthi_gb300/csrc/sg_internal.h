@@ -1,0 +1,148 @@
+// Internal declarations of the smuthi_gb300 CUDA library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/smuthi_gb300.h"
+
+struct sg_context;
+
+namespace sg {
+
+// ---------------------------------------------------------------- errors
+void set_error(const std::string &msg);
+void clear_error();
+
+struct Error {
+  int code;
+  std::string msg;
+};
+
+#define SG_CUDA(call)                                                                          \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess) throw ::sg::Error{SG_ERR_CUDA, std::string(#call) + ": " +          \
+                                                              cudaGetErrorString(e_)};          \
+  } while (0)
+
+#define SG_REQUIRE(cond, msg)                                   \
+  do {                                                          \
+    if (!(cond)) throw ::sg::Error{SG_ERR_ARG, std::string(msg)}; \
+  } while (0)
+
+// ---------------------------------------------------------------- device buffers
+template <typename T>
+struct DevBuf {
+  T *ptr = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    n = 0;
+  }
+  // grow-only allocation; contents are not preserved
+  void reserve(size_t count) {
+    if (count <= n && ptr) return;
+    release();
+    if (count == 0) return;
+    SG_CUDA(cudaMalloc(&ptr, count * sizeof(T)));
+    n = count;
+  }
+};
+
+// ---------------------------------------------------------------- coupling launch parameters
+// Vectors handled by the kernels are "padded": [particle][blocksize][nrhs] complex double.
+struct CouplingLaunch {
+  const double2 *pos;   // [N] particle (x, y)
+  const int *mofn;      // [bs]
+  const void *coef;     // [n_int][ncoef][bs][bs] complex (double2 or float2), n1 fastest
+  const int4 *pairs;    // FP32 path: [N][N] (k, t, cos phi, sin phi) or null
+  int n, bs, n_int, ncoef;
+  double rho_min, res;
+  const double2 *x;     // padded input
+  double2 *y;           // padded output (or split partials)
+  double2 *partial;     // [nsplit][N][bs][R] scratch when nsplit > 1
+  int nrhs;             // R (leading dimension of x, y)
+  int master;           // 0: y = W x; 1: y = x - T W x
+  const double2 *t;     // T blocks: diag [types][bs] or full [types][bs][bs]
+  const int *ptype;     // [N]
+  int t_diag;
+};
+
+// launch the coupling matvec on padded vectors; returns number of kernels launched
+int launch_coupling(const CouplingLaunch &L, bool fp32, int nsplit, cudaStream_t st);
+// padded-vector operator application and solver (sg_gmres.cu)
+void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool master, bool fp32, cudaStream_t st);
+void solve_padded(sg_context *c, const double2 *b, double2 *x, int R, double rtol, int restart, int maxiter,
+                  int precision, sg_solve_info *info, cudaStream_t st);
+void residual_norms(sg_context *c, const double2 *b, const double2 *x, int R, double *rel, cudaStream_t st);
+// choose the j-split for a problem (>= 1)
+int choose_split(int n_particles, int nrhs);
+
+// ---------------------------------------------------------------- table preparation
+// Build interpolation coefficients from a raw FP64 table [len_rho][bs][bs] (n2 fastest).
+void build_coefficients(int kind, const double2 *raw, int len_rho, int bs, double2 *coef64, float2 *coef32,
+                        double2 *work, cudaStream_t st);
+int coef_count(int kind);
+// FP32 per-pair data (interval index, t, cos, sin) for all ordered pairs.
+void build_pairs(const double2 *pos, int n, double rho_min, double res, int n_int, int4 *pairs, cudaStream_t st);
+
+// ---------------------------------------------------------------- BLAS-1 style kernels (padded vectors)
+void k_gather(const double2 *src, double2 *dst, const int *map, int n_unknowns, int nrhs, cudaStream_t st);
+void k_scatter(const double2 *src, double2 *dst, const int *map, int n_unknowns, int nrhs, cudaStream_t st);
+void k_zero(double2 *p, size_t n, cudaStream_t st);
+
+}  // namespace sg
+
+// ---------------------------------------------------------------- context
+struct sg_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+
+  // particles
+  int n = 0, bs = 0, n_unknowns = 0;
+  bool uniform = true;  // reference layout == padded layout
+  sg::DevBuf<double2> pos;
+  sg::DevBuf<int> map;  // [n_unknowns] -> padded index
+  sg::DevBuf<int> mofn;
+  std::vector<int> h_mofn;
+
+  // lookup
+  int kind = -1, len_rho = 0, n_int = 0, ncoef = 0;
+  double rho_min = 0, res = 0;
+  sg::DevBuf<double2> coef64;
+  sg::DevBuf<float2> coef32;
+  sg::DevBuf<int4> pairs;
+  bool pairs_ready = false;
+
+  // T-matrices
+  int n_types = 0, t_diag = 1;
+  sg::DevBuf<double2> tmat;
+  sg::DevBuf<int> ptype;
+  bool t_ready = false;
+
+  // work buffers
+  sg::DevBuf<double2> io_in, io_out, pad_in, pad_out, sol_b, sol_x;
+  sg::DevBuf<double2> w_partial, w_b, w_x, w_r, w_w, w_basis, w_tmp, w_d;
+  sg::DevBuf<double> w_red;
+  sg::DevBuf<double2> w_hcol;
+  std::vector<double> h_red;
+
+  // instrumentation
+  int64_t launches = 0;
+  bool profiling = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;
+  int64_t coupling_launches = 0;
+  double coupling_ms = 0.0;
+
+  size_t padded(int nrhs) const { return (size_t)n * bs * nrhs; }
+};

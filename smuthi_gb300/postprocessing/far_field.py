@@ -1,0 +1,171 @@
+"""Extinction and total scattering cross sections of plane-wave excitations.
+
+Mirrors ``extinction_cross_section`` (smuthi/postprocessing/far_field.py:517-654,
+extinction_direction='both') and ``total_scattering_cross_section`` (:480-514,
+via scattered_far_field :363-427 and pwe_to_ff_conversion :217-254). The
+reference converts every particle's outgoing SWE to a plane wave expansion and
+applies the layer response per particle (scattered_field.py:80-150,
+transformations.py:133-233). For particles in one layer the conversion is
+linear in the particles' coefficients, so here the particle sum is a matrix
+product (coefficients x angular factors x lateral phase) taken before the
+layer response, which is applied once.
+"""
+import numpy as np
+
+from .. import fields as flds
+from .. import layers as lay
+from ..fields.transformations import transformation_coefficients_vwf
+from ..utility.math import legendre_normalized
+
+
+def _particle_data(particle_list, coefficients=None):
+    z = {p.position[2] for p in particle_list}
+    lm = {(p.l_max, p.m_max) for p in particle_list}
+    if len(z) != 1 or len(lm) != 1:
+        raise NotImplementedError('cross sections are provided for particles at one height with one multipole cut-off')
+    l_max, m_max = lm.pop()
+    xy = np.array([p.position[:2] for p in particle_list], dtype=float)
+    if coefficients is None:
+        coefficients = np.array([p.scattered_field.coefficients for p in particle_list])
+    return xy, z.pop(), l_max, m_max, np.asarray(coefficients)
+
+
+def scattered_pwe(vacuum_wavelength, layer_system, xy, z, l_max, m_max, coefs, layer_number, kpar, alpha,
+                  chunk=16):
+    """(g_up, g_down) [nrhs, 2, K, A] of the scattered field in ``layer_number``.
+
+    coefs: [nrhs, N, blocksize] outgoing SWE coefficients (or [N, blocksize]).
+    """
+    coefs = np.asarray(coefs)
+    single = coefs.ndim == 2
+    if single:
+        coefs = coefs[None]
+    R = coefs.shape[0]
+    kpar = np.atleast_1d(np.asarray(kpar))
+    alpha = np.atleast_1d(np.asarray(alpha, dtype=float))
+    omega = flds.angular_frequency(vacuum_wavelength)
+    i_s = layer_system.layer_number(z)
+    k = omega * layer_system.refractive_indices[i_s]
+    kz = flds.k_z(k_parallel=kpar, k=k)
+    dz = layer_system.reference_z(i_s) - z
+    tau, ll, mm = flds.index_table(l_max, m_max)
+    nm = 2 * m_max + 1
+    gs = []
+    for sgn in (1, -1):  # up, down
+        _, pilm, taulm = legendre_normalized(sgn * kz / k, kpar / k, l_max)
+        # S[n, pol, K, m]: angular coefficient, nonzero only for m == m(n)
+        S = np.zeros((len(tau), 2, len(kpar), nm), complex)
+        for n in range(len(tau)):
+            for pol in range(2):
+                S[n, pol, :, mm[n] + m_max] = transformation_coefficients_vwf(tau[n], ll[n], mm[n], pol, pilm, taulm)
+        D = np.einsum('rin,npkm->rpkmi', coefs, S)  # [R, 2, K, m, N]
+        eima = np.exp(1j * np.outer(np.arange(-m_max, m_max + 1), alpha))  # [m, A]
+        g = np.zeros((R, 2, len(kpar), len(alpha)), complex)
+        for k0 in range(0, len(kpar), chunk):
+            ks = slice(k0, k0 + chunk)
+            kp = kpar[ks]
+            ph = np.exp(-1j * kp[:, None, None] * (np.cos(alpha)[None, :, None] * xy[None, None, :, 0]
+                                                   + np.sin(alpha)[None, :, None] * xy[None, None, :, 1]))
+            # sum over particles, then over m
+            F = np.einsum('kai,rpkmi->rpkam', ph, D[:, :, ks])
+            g[:, :, ks, :] = np.einsum('rpkam,ma->rpka', F, eima)
+        pref = np.exp(1j * sgn * kz * dz) / (2 * np.pi * kz * k)
+        gs.append(g * pref[None, None, :, None])
+    g_up, g_dn = gs
+    out_up = np.zeros_like(g_up)
+    out_dn = np.zeros_like(g_dn)
+    if i_s == layer_number:
+        out_up += g_up
+        out_dn += g_dn
+    for pol in range(2):
+        L = lay.layersystem_response_matrix(pol, layer_system.thicknesses, layer_system.refractive_indices, kpar,
+                                            omega, i_s, layer_number)
+        out_up[:, pol] += L[0, 0][None, :, None] * g_up[:, pol] + L[0, 1][None, :, None] * g_dn[:, pol]
+        out_dn[:, pol] += L[1, 0][None, :, None] * g_up[:, pol] + L[1, 1][None, :, None] * g_dn[:, pol]
+    if single:
+        return out_up[0], out_dn[0]
+    return out_up, out_dn
+
+
+def _incidence(initial_field, layer_system):
+    i_top = layer_system.number_of_layers() - 1
+    i_P = 0 if np.cos(initial_field.polar_angle) > 0 else i_top
+    n_P = layer_system.refractive_indices[i_P]
+    if np.imag(n_P):
+        raise ValueError('plane wave from absorbing layer: cross section undefined')
+    return i_P, float(np.real(n_P))
+
+
+def extinction_cross_section(simulation=None, initial_field=None, particle_list=None, layer_system=None,
+                             coefficients=None):
+    """Extinction cross section (top plus bottom extinction) of a plane wave."""
+    initial_field = initial_field or simulation.initial_field
+    particle_list = particle_list or simulation.particle_list
+    layer_system = layer_system or simulation.layer_system
+    if type(initial_field).__name__ != 'PlaneWave':
+        raise ValueError('Cross section only defined for plane wave excitation.')
+    xy, z, l_max, m_max, coefs = _particle_data(particle_list, coefficients)
+    i_top = layer_system.number_of_layers() - 1
+    lam = initial_field.vacuum_wavelength
+    omega = flds.angular_frequency(lam)
+    k_bot = omega * layer_system.refractive_indices[0]
+    k_top = omega * layer_system.refractive_indices[-1]
+    pol_P = initial_field.polarization
+    beta, alpha = initial_field.polar_angle, initial_field.azimuthal_angle
+    i_P, n_P = _incidence(initial_field, layer_system)
+    k_P = k_bot if i_P == 0 else k_top
+    kappa = np.sin(beta) * k_P
+    kvec = np.array([np.cos(alpha) * kappa, np.sin(alpha) * kappa, k_P * np.cos(beta)])
+    rvec = np.array([0, 0, layer_system.reference_z(i_P)]) - np.array(initial_field.reference_point)
+    A_P = initial_field.amplitude * np.exp(1j * np.dot(kvec, rvec))
+    I0 = abs(A_P) ** 2 * n_P / 2
+    g_top, _ = scattered_pwe(lam, layer_system, xy, z, l_max, m_max, coefs, i_top, kappa, alpha)
+    _, g_bot = scattered_pwe(lam, layer_system, xy, z, l_max, m_max, coefs, 0, kappa, alpha)
+    _, init_bot = initial_field.plane_wave_expansion(layer_system, 0)
+    init_top, _ = initial_field.plane_wave_expansion(layer_system, i_top)
+    kz_bot = flds.k_z(k_parallel=kappa, k=k_bot)
+    kz_top = flds.k_z(k_parallel=kappa, k=k_top)
+    p_bot = 4 * np.pi ** 2 * kz_bot / omega * (init_bot.coefficients[pol_P] * np.conj(g_bot[pol_P, 0, 0])).real
+    p_top = 4 * np.pi ** 2 * kz_top / omega * (init_top.coefficients[pol_P] * np.conj(g_top[pol_P, 0, 0])).real
+    return float(np.real(-p_bot / I0) + np.real(-p_top / I0))
+
+
+def total_scattering_cross_section(simulation=None, initial_field=None, particle_list=None, layer_system=None,
+                                   polar_angles='default', azimuthal_angles='default', angular_resolution=None,
+                                   coefficients=None):
+    """Angle-integrated scattering cross section (trapezoidal rule over the far-field grid)."""
+    initial_field = initial_field or simulation.initial_field
+    particle_list = particle_list or simulation.particle_list
+    layer_system = layer_system or simulation.layer_system
+    if angular_resolution is not None:
+        az, po = flds.angular_arrays(angular_resolution)
+    else:
+        az = flds.default_azimuthal_angles if isinstance(azimuthal_angles, str) else azimuthal_angles
+        po = flds.default_polar_angles if isinstance(polar_angles, str) else polar_angles
+        if az is None or po is None:
+            az, po = flds.angular_arrays()
+    xy, z, l_max, m_max, coefs = _particle_data(particle_list, coefficients)
+    lam = initial_field.vacuum_wavelength
+    omega = flds.angular_frequency(lam)
+    _, n_P = _incidence(initial_field, layer_system)
+    I0 = abs(initial_field.amplitude) ** 2 * n_P / 2
+    i_top = layer_system.number_of_layers() - 1
+    parts = []
+    for layer, sel, up in ((i_top, po[po < np.pi / 2], True), (0, po[po > np.pi / 2], False)):
+        n_l = layer_system.refractive_indices[layer]
+        if len(sel) <= 1 or np.imag(n_l) != 0:
+            continue
+        kp = np.sort(np.sin(sel) * n_l) * omega
+        gu, gd = scattered_pwe(lam, layer_system, xy, z, l_max, m_max, coefs, layer, kp, az)
+        g = gu if up else gd
+        k = omega * n_l
+        polar = np.arcsin(kp / k) if up else np.pi - np.arcsin(kp / k)
+        kz = flds.k_z(k_parallel=kp, k=k)
+        intens = (2 * np.pi ** 2 / omega * (kz ** 2 * k)[None, :, None] * abs(g) ** 2).real
+        order = np.argsort(polar)
+        parts.append((np.real(polar[order]), intens[:, order, :]))
+    parts.sort(key=lambda p: p[0][0])
+    polar = np.concatenate([p[0] for p in parts])
+    sig = np.concatenate([p[1] for p in parts], axis=1) / I0
+    per_pol = np.trapezoid(np.trapezoid(sig, az[None, None, :]) * np.sin(polar[None, :]), polar[None, :])
+    return float(per_pol[0] + per_pol[1])
