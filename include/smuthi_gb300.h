@@ -97,11 +97,12 @@ typedef struct sg_solve_info {
   int32_t converged;       /* number of rhs that met the tolerance */
   int32_t reserved;
   double max_rel_residual; /* max over rhs of ||b - M x|| / ||b|| (FP64 operator) */
-  double seconds;          /* wall time of the solve on the device */
+  double seconds;          /* host wall time of the solve call */
+  double device_seconds;   /* CUDA-event time of the solve on the context's stream */
 } sg_solve_info;
 
 /* GMRES(restart) on the master operator, scipy semantics of the call at
- * smuthi/linearsystem/linear_system.py:285 (x0 = given x, restart default 20,
+ * smuthi/linearsystem/linear_system.py:285 (x0 = given x, restart default 20, at most 128,
  * stop when ||b - M x|| <= rtol ||b||, explicit residual at every restart).
  * b, x: host buffers n_unknowns x nrhs; x holds x0 on entry and the solution
  * on return. nrhs > 1 runs independent Krylov spaces in lockstep, sharing one
@@ -121,11 +122,17 @@ int sg_true_residual(sg_context *ctx, const double *b, const double *x, int nrhs
 /* Kernel instrumentation. sg_profile(ctx, 1) brackets every coupling-kernel
  * launch with CUDA events on its stream; sg_kernel_timing synchronises and
  * returns the summed event time (ms) and the number of bracketed launches
- * since the last reset. sg_launch_count returns the number of kernels this
- * context has launched since it was created. */
+ * of the given precision (SG_FP64, SG_FP32, or -1 for both) since the last
+ * reset. sg_launch_count returns the number of kernels this context has
+ * launched since it was created. */
 int sg_profile(sg_context *ctx, int enable);
-int sg_kernel_timing(sg_context *ctx, double *total_ms, int64_t *count, int reset);
+int sg_kernel_timing(sg_context *ctx, int precision, double *total_ms, int64_t *count, int reset);
 int sg_launch_count(sg_context *ctx, int64_t *count);
+
+/* FMA throughput (TFLOP/s, 2 flops per FMA) of the FP64 or FP32 pipe of the
+ * context's device, measured with a dependent-chain probe kernel. Used to
+ * state pipe rooflines; no counterpart in the reference. */
+int sg_measure_fma_peak(sg_context *ctx, int precision, double *tflops);
 
 #ifdef __cplusplus
 }

@@ -23,7 +23,7 @@ KINDS = {"linear": SG_LINEAR, "cubic": SG_CUBIC, "cubic_hermite": SG_CUBIC_HERMI
 EXPORTS = ("sg_last_error", "sg_version", "sg_create", "sg_destroy", "sg_set_particles", "sg_set_lookup",
            "sg_set_tmatrix", "sg_coupling_matvec", "sg_master_matvec", "sg_coupling_matvec_dev",
            "sg_master_matvec_dev", "sg_gmres_solve", "sg_gmres_solve_dev", "sg_true_residual", "sg_profile",
-           "sg_kernel_timing", "sg_launch_count")
+           "sg_kernel_timing", "sg_launch_count", "sg_measure_fma_peak")
 
 
 class LibraryMissing(RuntimeError):
@@ -43,7 +43,8 @@ class NotConverged(SmuthiGB300Error):
 class SolveInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("restarts", ctypes.c_int32), ("fp64_matvecs", ctypes.c_int32),
                 ("fp32_matvecs", ctypes.c_int32), ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32),
-                ("max_rel_residual", ctypes.c_double), ("seconds", ctypes.c_double)]
+                ("max_rel_residual", ctypes.c_double), ("seconds", ctypes.c_double),
+                ("device_seconds", ctypes.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
@@ -72,8 +73,9 @@ def _declare(L):
         "sg_gmres_solve_dev": [_P, _P, _P, _I, _D, _I, _I, _I, ctypes.POINTER(SolveInfo), _P],
         "sg_true_residual": [_P, _P, _P, _I, _P],
         "sg_profile": [_P, _I],
-        "sg_kernel_timing": [_P, ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_int64), _I],
+        "sg_kernel_timing": [_P, _I, ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_int64), _I],
         "sg_launch_count": [_P, ctypes.POINTER(ctypes.c_int64)],
+        "sg_measure_fma_peak": [_P, _I, ctypes.POINTER(_D)],
     }
     for name, args in sigs.items():
         fn = getattr(L, name)
@@ -202,11 +204,17 @@ class Context:
     def profile(self, enable=True):
         check(lib().sg_profile(self.h, 1 if enable else 0))
 
-    def kernel_timing(self, reset=True):
+    def kernel_timing(self, precision=-1, reset=True):
+        """(summed ms, launches) of profiled coupling kernels of a precision (-1: both)."""
         ms = ctypes.c_double()
         n = ctypes.c_int64()
-        check(lib().sg_kernel_timing(self.h, ctypes.byref(ms), ctypes.byref(n), 1 if reset else 0))
+        check(lib().sg_kernel_timing(self.h, int(precision), ctypes.byref(ms), ctypes.byref(n), 1 if reset else 0))
         return ms.value, n.value
+
+    def fma_peak(self, precision):
+        out = ctypes.c_double()
+        check(lib().sg_measure_fma_peak(self.h, int(precision), ctypes.byref(out)))
+        return out.value
 
     def launch_count(self):
         n = ctypes.c_int64()

@@ -92,8 +92,8 @@ int sg_destroy(sg_context *ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (auto &ev : ctx->events) {
-      cudaEventDestroy(ev.first);
-      cudaEventDestroy(ev.second);
+      cudaEventDestroy(ev.e0);
+      cudaEventDestroy(ev.e1);
     }
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -317,7 +317,7 @@ static int solve_dev_impl(sg_context *ctx, const double2 *b, double2 *x, int nrh
   require_ready(ctx, true);
   SG_REQUIRE(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
   SG_REQUIRE(rtol > 0 && std::isfinite(rtol), "rtol must be positive");
-  SG_REQUIRE(restart >= 0 && restart <= 64, "restart must be in [0, 64] (0 = 20)");
+  SG_REQUIRE(restart >= 0 && restart <= 128, "restart must be in [0, 128] (0 = 20)");
   SG_REQUIRE(precision == SG_FP64 || precision == SG_FP32, "unknown precision");
   use_device(ctx);
   if (precision == SG_FP32) ensure_pairs(ctx, st);
@@ -408,26 +408,45 @@ int sg_profile(sg_context *ctx, int enable) {
   });
 }
 
-int sg_kernel_timing(sg_context *ctx, double *total_ms, int64_t *count, int reset) {
+int sg_kernel_timing(sg_context *ctx, int precision, double *total_ms, int64_t *count, int reset) {
   return guarded([&]() -> int {
     SG_REQUIRE(ctx != nullptr, "null context");
+    SG_REQUIRE(precision >= -1 && precision <= 1, "precision must be SG_FP64, SG_FP32 or -1 (both)");
     use_device(ctx);
     for (auto &ev : ctx->events) {
-      SG_CUDA(cudaEventSynchronize(ev.second));
+      SG_CUDA(cudaEventSynchronize(ev.e1));
       float ms = 0.f;
-      SG_CUDA(cudaEventElapsedTime(&ms, ev.first, ev.second));
-      ctx->coupling_ms += ms;
-      ctx->coupling_launches += 1;
-      cudaEventDestroy(ev.first);
-      cudaEventDestroy(ev.second);
+      SG_CUDA(cudaEventElapsedTime(&ms, ev.e0, ev.e1));
+      ctx->coupling_ms[ev.fp32] += ms;
+      ctx->coupling_launches[ev.fp32] += 1;
+      cudaEventDestroy(ev.e0);
+      cudaEventDestroy(ev.e1);
     }
     ctx->events.clear();
-    if (total_ms) *total_ms = ctx->coupling_ms;
-    if (count) *count = ctx->coupling_launches;
-    if (reset) {
-      ctx->coupling_ms = 0.0;
-      ctx->coupling_launches = 0;
+    const int lo = precision < 0 ? 0 : precision, hi = precision < 0 ? 1 : precision;
+    double ms = 0.0;
+    int64_t n = 0;
+    for (int p = lo; p <= hi; ++p) {
+      ms += ctx->coupling_ms[p];
+      n += ctx->coupling_launches[p];
     }
+    if (total_ms) *total_ms = ms;
+    if (count) *count = n;
+    if (reset) {
+      ctx->coupling_ms[0] = ctx->coupling_ms[1] = 0.0;
+      ctx->coupling_launches[0] = ctx->coupling_launches[1] = 0;
+    }
+    return SG_OK;
+  });
+}
+
+int sg_measure_fma_peak(sg_context *ctx, int precision, double *tflops) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx && tflops, "null argument");
+    SG_REQUIRE(precision == SG_FP64 || precision == SG_FP32, "unknown precision");
+    use_device(ctx);
+    *tflops = sg::fma_peak(precision == SG_FP64 ? 1 : 0, ctx->stream);
+    ctx->launches += 4;
     return SG_OK;
   });
 }

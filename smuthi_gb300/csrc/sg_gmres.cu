@@ -22,7 +22,7 @@
 namespace sg {
 
 typedef std::complex<double> cd;
-static constexpr int kMaxVec = 66;  // restart <= 64, plus w and one spare
+static constexpr int kMaxVec = 130;  // restart <= 128, plus w and one spare
 static constexpr int kHcol = 2 * kMaxVec + 4;  // per-rhs slots of the Arnoldi scalar buffer
 
 struct VecList {
@@ -212,12 +212,15 @@ struct GmresResult {
 };
 
 // Lockstep GMRES on padded device vectors. b, x: len(); x holds x0 (zero_x0 = x0 is zero).
+// stall_cycles > 0 stops a right-hand side whose explicit residual fell by less than 5% over that many
+// consecutive restart cycles (used for the FP32-operator correction solves, whose residual has a noise
+// floor near the FP32 operator error); 0 keeps scipy's semantics.
 static GmresResult gmres_lockstep(Solver &S, const double2 *b, double2 *x, double rtol, int restart, int maxiter,
-                                  bool fp32, bool zero_x0, const std::vector<char> &skip) {
+                                  bool fp32, bool zero_x0, const std::vector<char> &skip, int stall_cycles = 0) {
   sg_context *c = S.c;
   const int R = S.R;
   const size_t len = S.len();
-  restart = std::max(1, std::min(restart, (int)std::min<size_t>(S.rows, 64)));
+  restart = std::max(1, std::min(restart, (int)std::min<size_t>(S.rows, kMaxVec - 2)));
   c->w_basis.reserve((size_t)(restart + 1) * len);
   c->w_w.reserve(len);
   c->w_r.reserve(len);
@@ -250,7 +253,16 @@ static GmresResult gmres_lockstep(Solver &S, const double2 *b, double2 *x, doubl
       res.conv[q] = 1;
     }
   }
-  // r = b - M x0
+  // r = b - M x0; like scipy, an all-zero x0 skips the operator application
+  if (!zero_x0) {
+    L1.v[0] = x;
+    S.dots(L1, 1, x, dh);
+    SG_CUDA(cudaMemcpyAsync(hb.data(), dh, R * sizeof(double2), cudaMemcpyDeviceToHost, S.st));
+    SG_CUDA(cudaStreamSynchronize(S.st));
+    bool allzero = true;
+    for (int q = 0; q < R; ++q) allzero &= hb[q].x == 0.0;
+    zero_x0 = allzero;
+  }
   if (zero_x0) {
     SG_CUDA(cudaMemcpyAsync(r, b, len * sizeof(double2), cudaMemcpyDeviceToDevice, S.st));
   } else {
@@ -278,6 +290,7 @@ static GmresResult gmres_lockstep(Solver &S, const double2 *b, double2 *x, doubl
   std::vector<double> hscale(R), hmask(R);
   std::vector<int> colstop(R);
   std::vector<char> inner_done(R), breakdown(R);
+  std::vector<int> stalls(R, 0);
   int inner_iter = 0;
   c->w_d.reserve(len);
 
@@ -415,6 +428,7 @@ static GmresResult gmres_lockstep(Solver &S, const double2 *b, double2 *x, doubl
     SG_CUDA(cudaMemcpyAsync(hb.data(), dh, R * sizeof(double2), cudaMemcpyDeviceToHost, S.st));
     SG_CUDA(cudaStreamSynchronize(S.st));
     for (int q = 0; q < R; ++q) {
+      const double before = rnorm[q];
       rnorm[q] = std::sqrt(std::max(0.0, hb[q].x));
       if (!active[q]) continue;
       if (rnorm[q] <= atol[q]) {
@@ -425,6 +439,14 @@ static GmresResult gmres_lockstep(Solver &S, const double2 *b, double2 *x, doubl
       if (breakdown[q]) {
         active[q] = 0;
         continue;
+      }
+      if (stall_cycles > 0) {
+        const double ref = cycle == 0 ? bnrm[q] : before;
+        stalls[q] = (rnorm[q] > 0.95 * ref) ? stalls[q] + 1 : 0;
+        if (stalls[q] >= stall_cycles) {
+          active[q] = 0;
+          continue;
+        }
       }
       if (presid[q] <= ptol[q]) pfac[q] = std::max(eps, 0.25 * pfac[q]);
       else pfac[q] = std::min(1.0, 1.5 * pfac[q]);
@@ -465,13 +487,25 @@ static GmresResult refine_mixed(Solver &S, const double2 *b, double2 *x, double 
   std::vector<char> done(R, 0);
   std::vector<double> mask(R);
   const int max_steps = 40;
-  int inner_total = 0;
+  const int inner_cap_cycles = std::max(4, 4000 / std::max(1, restart));  // <= ~4000 iterations per correction
+  int inner_total = 0, no_progress = 0;
+  double prev_worst = 0.0;
+  L1.v[0] = x;
+  S.dots(L1, 1, x, dh);
+  SG_CUDA(cudaMemcpyAsync(hb.data(), dh, R * sizeof(double2), cudaMemcpyDeviceToHost, S.st));
+  SG_CUDA(cudaStreamSynchronize(S.st));
+  bool x0_zero = true;
+  for (int q = 0; q < R; ++q) x0_zero &= hb[q].x == 0.0;
   for (steps = 0; steps <= max_steps; ++steps) {
-    // FP64 true residual
-    S.master(x, rr, false);
-    fp64_mv++;
-    sub_from_kernel<<<nblocks(len), 256, 0, S.st>>>(b, rr, len);
-    SG_CUDA(cudaGetLastError());
+    // FP64 true residual (r = b exactly when x0 == 0)
+    if (steps == 0 && x0_zero) {
+      SG_CUDA(cudaMemcpyAsync(rr, b, len * sizeof(double2), cudaMemcpyDeviceToDevice, S.st));
+    } else {
+      S.master(x, rr, false);
+      fp64_mv++;
+      sub_from_kernel<<<nblocks(len), 256, 0, S.st>>>(b, rr, len);
+      SG_CUDA(cudaGetLastError());
+    }
     L1.v[0] = rr;
     S.dots(L1, 1, rr, dh);
     SG_CUDA(cudaMemcpyAsync(hb.data(), dh, R * sizeof(double2), cudaMemcpyDeviceToHost, S.st));
@@ -487,12 +521,19 @@ static GmresResult refine_mixed(Solver &S, const double2 *b, double2 *x, double 
       if (!done[q]) worst = std::max(worst, rel);
     }
     if (worst == 0.0 || steps == max_steps || inner_total >= maxiter) break;
+    // refinement must contract the FP64 residual; two steps without halving it end the solve
+    if (steps > 0 && worst > 0.5 * prev_worst) {
+      if (++no_progress >= 2) break;
+    } else {
+      no_progress = 0;
+    }
+    prev_worst = worst;
     // correction solve with the FP32 operator: tolerance relative to the current residual
     double tau = 0.3 * rtol / worst;
     tau = std::max(1e-6, std::min(0.5, tau));
     k_zero(d, len, S.st);
-    GmresResult g = gmres_lockstep(S, rr, d, tau, restart, std::max(1, (maxiter - inner_total) / restart + 1), true,
-                                   true, done);
+    const int cycles = std::max(1, std::min(inner_cap_cycles, (maxiter - inner_total) / restart + 1));
+    GmresResult g = gmres_lockstep(S, rr, d, tau, restart, cycles, true, true, done, 2);
     fp32_mv += g.matvecs;
     inner_total += g.inner_iters;
     out.inner_iters += g.inner_iters;
@@ -514,6 +555,10 @@ void solve_padded(sg_context *c, const double2 *b, double2 *x, int R, double rto
   if (maxiter <= 0) maxiter = 10 * c->n_unknowns;
   if (restart <= 0) restart = 20;
   const auto t0 = std::chrono::steady_clock::now();
+  cudaEvent_t ev0, ev1;
+  SG_CUDA(cudaEventCreate(&ev0));
+  SG_CUDA(cudaEventCreate(&ev1));
+  SG_CUDA(cudaEventRecord(ev0, st));
   GmresResult g;
   int fp64_mv = 0, fp32_mv = 0, steps = 0;
   if (precision == SG_FP32) {
@@ -523,8 +568,13 @@ void solve_padded(sg_context *c, const double2 *b, double2 *x, int R, double rto
     fp64_mv = g.matvecs;
     steps = g.cycles;
   }
+  SG_CUDA(cudaEventRecord(ev1, st));
   SG_CUDA(cudaStreamSynchronize(st));
   const auto t1 = std::chrono::steady_clock::now();
+  float dev_ms = 0.f;
+  SG_CUDA(cudaEventElapsedTime(&dev_ms, ev0, ev1));
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
   if (info) {
     info->iterations = g.inner_iters;
     info->restarts = steps;
@@ -540,6 +590,7 @@ void solve_padded(sg_context *c, const double2 *b, double2 *x, int R, double rto
     info->reserved = 0;
     info->max_rel_residual = mx;
     info->seconds = std::chrono::duration<double>(t1 - t0).count();
+    info->device_seconds = dev_ms * 1e-3;
   }
 }
 
@@ -577,7 +628,7 @@ void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool maste
   c->launches += launch_coupling(L, fp32, ns, st);
   if (c->profiling) {
     SG_CUDA(cudaEventRecord(e1, st));
-    c->events.push_back({e0, e1});
+    c->events.push_back({e0, e1, fp32 ? 1 : 0});
   }
 }
 

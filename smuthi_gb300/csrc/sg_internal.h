@@ -100,6 +100,9 @@ void k_gather(const double2 *src, double2 *dst, const int *map, int n_unknowns, 
 void k_scatter(const double2 *src, double2 *dst, const int *map, int n_unknowns, int nrhs, cudaStream_t st);
 void k_zero(double2 *p, size_t n, cudaStream_t st);
 
+// FMA-throughput probe (TFLOP/s) of the FP64 or FP32 pipe
+double fma_peak(int fp64, cudaStream_t st);
+
 }  // namespace sg
 
 // ---------------------------------------------------------------- context
@@ -140,9 +143,13 @@ struct sg_context {
   // instrumentation
   int64_t launches = 0;
   bool profiling = false;
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;
-  int64_t coupling_launches = 0;
-  double coupling_ms = 0.0;
+  struct Timed {
+    cudaEvent_t e0, e1;
+    int fp32;
+  };
+  std::vector<Timed> events;
+  int64_t coupling_launches[2] = {0, 0};  // [fp64, fp32]
+  double coupling_ms[2] = {0.0, 0.0};
 
   size_t padded(int nrhs) const { return (size_t)n * bs * nrhs; }
 };

@@ -26,16 +26,40 @@ from ...fields.transformations import ab5_coefficients, ipow, transformation_coe
 from ...utility.math import legendre_normalized, spherical_hankel
 
 
-def radial_grid(particle_xy, resolution):
+def pair_distance_extremes(particle_xy):
+    """(largest, smallest nonzero-index) pair distance of lateral positions.
+
+    The largest distance is attained between convex-hull vertices and the
+    smallest between nearest neighbours, so neither needs the N x N matrix;
+    both are evaluated with the same sqrt(dx^2 + dy^2) as a full matrix would.
+    """
     xy = np.asarray(particle_xy, dtype=float)
-    d2 = np.zeros((len(xy), len(xy)))
-    for c in range(2):
-        d = xy[:, None, c] - xy[None, :, c]
-        d2 += d * d
-    rho_pp = np.sqrt(d2)
-    grid = np.arange(-3 * resolution, rho_pp.max() + 3 * resolution, resolution)
-    off = rho_pp[~np.eye(len(xy), dtype=bool)]
-    return grid, (off.min() if off.size else np.inf)
+    n = len(xy)
+    if n < 2:
+        return 0.0, np.inf
+    if n <= 64:
+        d = np.sqrt((xy[:, None, 0] - xy[None, :, 0]) ** 2 + (xy[:, None, 1] - xy[None, :, 1]) ** 2)
+        return float(d.max()), float(d[~np.eye(n, dtype=bool)].min())
+    from scipy.spatial import ConvexHull, cKDTree
+    try:
+        hull = xy[ConvexHull(xy).vertices]
+    except Exception:  # degenerate (collinear) sets: fall back to all points
+        hull = xy
+    dmax = 0.0
+    for s in range(0, len(hull), 1024):
+        h = hull[s:s + 1024]
+        d = np.sqrt((h[:, None, 0] - hull[None, :, 0]) ** 2 + (h[:, None, 1] - hull[None, :, 1]) ** 2)
+        dmax = max(dmax, float(d.max()))
+    _, idx = cKDTree(xy).query(xy, k=2)
+    j = idx[:, 1]
+    dmin = float(np.sqrt((xy[:, 0] - xy[j, 0]) ** 2 + (xy[:, 1] - xy[j, 1]) ** 2).min())
+    return dmax, dmin
+
+
+def radial_grid(particle_xy, resolution):
+    """Radial grid arange(-3 r, rho_max + 3 r, r) and the smallest particle distance."""
+    dmax, dmin = pair_distance_extremes(particle_xy)
+    return np.arange(-3 * resolution, dmax + 3 * resolution, resolution), dmin
 
 
 def direct_part(k_is, rho, l_max, m_max, rho_min_pair):
