@@ -134,6 +134,22 @@ int sg_launch_count(sg_context *ctx, int64_t *count);
  * state pipe rooflines; no counterpart in the reference. */
 int sg_measure_fma_peak(sg_context *ctx, int precision, double *tflops);
 
+/* Allocation-free FP64 coupling matvec y = W x with linear interpolation, for callers that
+ * cannot call cudaMalloc while they compute (code running inside another framework's device
+ * memory pool, or loops with a fixed memory budget after start-up). No counterpart in the
+ * reference. Every argument is a caller-owned device buffer: xy = double2[n_particles] lateral
+ * positions, m_of_n = int32[blocksize], table = complex128[len_rho][blocksize][blocksize] on the
+ * grid rho_k = rho_min + k * resolution (the reference layout; it must cover every particle
+ * distance), x, y = complex128[n_particles][blocksize][nrhs] (uniform blocks). The call allocates
+ * nothing: its scratch is a static 16 MiB device array held by every device that loads the
+ * library until exit, so n_particles * blocksize * nrhs must be <= 1048576 (larger sizes return
+ * SG_ERR_ARG). The first call on a device looks the array up (do it before any stream capture);
+ * `device` must be the current device. Calls that overlap on the GPU race on the shared scratch.
+ * Asynchronous on `stream` (a cudaStream_t, NULL = legacy default stream). */
+int sg_coupling_matvec_linear_noalloc(int device, int n_particles, const void *xy, int blocksize,
+                                      const void *m_of_n, int len_rho, double rho_min, double resolution,
+                                      const void *table, const void *x, void *y, int nrhs, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

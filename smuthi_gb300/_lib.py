@@ -23,7 +23,8 @@ KINDS = {"linear": SG_LINEAR, "cubic": SG_CUBIC, "cubic_hermite": SG_CUBIC_HERMI
 EXPORTS = ("sg_last_error", "sg_version", "sg_create", "sg_destroy", "sg_set_particles", "sg_set_lookup",
            "sg_set_tmatrix", "sg_coupling_matvec", "sg_master_matvec", "sg_coupling_matvec_dev",
            "sg_master_matvec_dev", "sg_gmres_solve", "sg_gmres_solve_dev", "sg_true_residual", "sg_profile",
-           "sg_kernel_timing", "sg_launch_count", "sg_measure_fma_peak")
+           "sg_kernel_timing", "sg_launch_count", "sg_measure_fma_peak",
+           "sg_coupling_matvec_linear_noalloc")
 
 
 class LibraryMissing(RuntimeError):
@@ -76,6 +77,7 @@ def _declare(L):
         "sg_kernel_timing": [_P, _I, ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_int64), _I],
         "sg_launch_count": [_P, ctypes.POINTER(ctypes.c_int64)],
         "sg_measure_fma_peak": [_P, _I, ctypes.POINTER(_D)],
+        "sg_coupling_matvec_linear_noalloc": [_I, _I, _P, _I, _P, _I, _D, _D, _P, _P, _P, _I, _P],
     }
     for name, args in sigs.items():
         fn = getattr(L, name)
