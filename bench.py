@@ -292,7 +292,10 @@ def run_ours(args, rank, world, local_rank):
         "chosen_form": {"iterations": infos[-1]["iterations"], "fp64_matvecs": infos[-1]["fp64_matvecs"],
                         "fp32_matvecs": infos[-1]["fp32_matvecs"], "refinement_steps": infos[-1]["restarts"],
                         "max_rel_residual_fp64": float(relres.max()), "learned_preconditioner": False,
-                        "batched": True, "x0": "0"},
+                        "batched": True, "x0": "0",
+                        "fp32_kernel": dict(zip(("variant", "ms_per_receiver", "ms_bucketed"),
+                                                ctx.fp32_autotune(R))),
+                        "fp32_kernel_variants": "0 = per-receiver, 1 = interval-bucketed (autotuned)"},
         "prep_s": round(prep_s, 2),
         "e2e": {"value": round(e2e_value, 6), "unit": UNIT, "h2d_bytes_per_step": int(2 * rhs.nbytes),
                 "d2h_bytes_per_step": int(rhs.nbytes)},

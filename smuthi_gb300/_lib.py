@@ -23,7 +23,7 @@ KINDS = {"linear": SG_LINEAR, "cubic": SG_CUBIC, "cubic_hermite": SG_CUBIC_HERMI
 EXPORTS = ("sg_last_error", "sg_version", "sg_create", "sg_destroy", "sg_set_particles", "sg_set_lookup",
            "sg_set_tmatrix", "sg_coupling_matvec", "sg_master_matvec", "sg_coupling_matvec_dev",
            "sg_master_matvec_dev", "sg_gmres_solve", "sg_gmres_solve_dev", "sg_true_residual", "sg_profile",
-           "sg_kernel_timing", "sg_launch_count", "sg_measure_fma_peak",
+           "sg_kernel_timing", "sg_launch_count", "sg_measure_fma_peak", "sg_fp32_autotune",
            "sg_coupling_matvec_linear_noalloc")
 
 
@@ -77,6 +77,7 @@ def _declare(L):
         "sg_kernel_timing": [_P, _I, ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_int64), _I],
         "sg_launch_count": [_P, ctypes.POINTER(ctypes.c_int64)],
         "sg_measure_fma_peak": [_P, _I, ctypes.POINTER(_D)],
+        "sg_fp32_autotune": [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D)],
         "sg_coupling_matvec_linear_noalloc": [_I, _I, _P, _I, _P, _I, _D, _D, _P, _P, _P, _I, _P],
     }
     for name, args in sigs.items():
@@ -217,6 +218,14 @@ class Context:
         out = ctypes.c_double()
         check(lib().sg_measure_fma_peak(self.h, int(precision), ctypes.byref(out)))
         return out.value
+
+    def fp32_autotune(self, nrhs):
+        """(variant, ms per-receiver, ms bucketed) chosen for an RHS count, variant -1 if not tuned."""
+        v = ctypes.c_int()
+        a = ctypes.c_double()
+        b = ctypes.c_double()
+        check(lib().sg_fp32_autotune(self.h, int(nrhs), ctypes.byref(v), ctypes.byref(a), ctypes.byref(b)))
+        return v.value, a.value, b.value
 
     def launch_count(self):
         n = ctypes.c_int64()

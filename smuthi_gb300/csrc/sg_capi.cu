@@ -42,11 +42,19 @@ static void require_ready(sg_context *c, bool need_t) {
   if (need_t) SG_REQUIRE(c->t_ready, "sg_set_tmatrix has not been called");
 }
 
+// FP32 operator data: the pair table of the per-receiver kernel and, when the sizes allow it, the
+// interval-bucketed plan; the autotuner picks between the two kernels per RHS count.
 static void ensure_pairs(sg_context *c, cudaStream_t st) {
   if (c->pairs_ready) return;
   c->pairs.reserve((size_t)c->n * c->n);
   sg::build_pairs(c->pos.ptr, c->n, c->rho_min, c->res, c->n_int, c->pairs.ptr, st);
   c->launches += 1;
+  c->use_bucket = false;
+  if (sg::bucket_supported(c)) {
+    sg::build_bucket_plan(c, st);
+    c->use_bucket = true;
+  }
+  c->tuned.clear();
   c->pairs_ready = true;
 }
 
@@ -447,6 +455,21 @@ int sg_measure_fma_peak(sg_context *ctx, int precision, double *tflops) {
     use_device(ctx);
     *tflops = sg::fma_peak(precision == SG_FP64 ? 1 : 0, ctx->stream);
     ctx->launches += 4;
+    return SG_OK;
+  });
+}
+
+int sg_fp32_autotune(sg_context *ctx, int nrhs, int *variant, double *ms_receiver, double *ms_bucket) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx && variant, "null argument");
+    for (const auto &t : ctx->tuned)
+      if (t.nrhs == nrhs) {
+        *variant = t.variant;
+        if (ms_receiver) *ms_receiver = t.ms_receiver;
+        if (ms_bucket) *ms_bucket = t.ms_bucket;
+        return SG_OK;
+      }
+    *variant = -1;
     return SG_OK;
   });
 }

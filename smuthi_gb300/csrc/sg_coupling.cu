@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kThreads) coupling_kernel(const CouplingLaunch
           cplx u;
           u.x = ph_re[q] * xr - ph_im[q] * xim;
           u.y = ph_re[q] * xim + ph_im[q] * xr;
-          ubuf[nrow[q] * RT + r] = u;
+          ubuf[r * bs + nrow[q]] = u;  // [r][n2]: lane-consecutive writes
         }
       }
     }
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(kThreads) coupling_kernel(const CouplingLaunch
     for (int n2 = 0; n2 < bs; ++n2) {
       cplx u[RT];
 #pragma unroll
-      for (int r = 0; r < RT; ++r) u[r] = ubuf[n2 * RT + r];
+      for (int r = 0; r < RT; ++r) u[r] = ubuf[r * bs + n2];
 #pragma unroll
       for (int q = 0; q < P; ++q) {
         const cplx *cp = cbase + (size_t)n2 * bs + nrowc[q];

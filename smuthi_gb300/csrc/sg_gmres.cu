@@ -595,12 +595,15 @@ void solve_padded(sg_context *c, const double2 *b, double2 *x, int R, double rto
 }
 
 // y = M x or W x on padded vectors (public matvec entry points)
-void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool master, bool fp32, cudaStream_t st) {
+// One CUDA-event-timed run of each FP32 kernel on the live operands; the faster one is cached per
+// RHS count. Runs once per (context, nrhs) and synchronises the stream, so it must not be reached
+// inside a stream capture.
+static void launch_receiver_fp32(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st) {
   CouplingLaunch L{};
   L.pos = c->pos.ptr;
   L.mofn = c->mofn.ptr;
-  L.coef = fp32 ? (const void *)c->coef32.ptr : (const void *)c->coef64.ptr;
-  L.pairs = fp32 ? c->pairs.ptr : nullptr;
+  L.coef = c->coef32.ptr;
+  L.pairs = c->pairs.ptr;
   L.n = c->n;
   L.bs = c->bs;
   L.n_int = c->n_int;
@@ -619,13 +622,73 @@ void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool maste
     c->w_partial.reserve((size_t)ns * c->n * c->bs * R);
     L.partial = c->w_partial.ptr;
   }
+  c->launches += launch_coupling(L, true, ns, st);
+}
+
+static int autotune_fp32(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st) {
+  cudaEvent_t e[4];
+  for (auto &ev : e) SG_CUDA(cudaEventCreate(&ev));
+  // warm both paths once (first launches carry one-time set-up costs), then time one run each
+  launch_receiver_fp32(c, x, y, R, master, st);
+  c->launches += launch_bucket_matvec(c, x, y, R, master, st);
+  SG_CUDA(cudaEventRecord(e[0], st));
+  launch_receiver_fp32(c, x, y, R, master, st);
+  SG_CUDA(cudaEventRecord(e[1], st));
+  SG_CUDA(cudaEventRecord(e[2], st));
+  c->launches += launch_bucket_matvec(c, x, y, R, master, st);
+  SG_CUDA(cudaEventRecord(e[3], st));
+  SG_CUDA(cudaEventSynchronize(e[3]));
+  float ms0 = 0.f, ms1 = 0.f;
+  SG_CUDA(cudaEventElapsedTime(&ms0, e[0], e[1]));
+  SG_CUDA(cudaEventElapsedTime(&ms1, e[2], e[3]));
+  for (auto &ev : e) cudaEventDestroy(ev);
+  const int v = ms1 < ms0 ? 1 : 0;
+  c->tuned.push_back({R, v, ms0, ms1});
+  return v;
+}
+
+void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool master, bool fp32, cudaStream_t st) {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (c->profiling) {
     SG_CUDA(cudaEventCreate(&e0));
     SG_CUDA(cudaEventCreate(&e1));
     SG_CUDA(cudaEventRecord(e0, st));
   }
-  c->launches += launch_coupling(L, fp32, ns, st);
+  int variant = 0;
+  if (fp32 && c->use_bucket) {
+    variant = -1;
+    for (const auto &t : c->tuned)
+      if (t.nrhs == R) variant = t.variant;
+    if (variant < 0) variant = autotune_fp32(c, x, y, R, master, st);
+  }
+  if (variant == 1) {
+    c->launches += launch_bucket_matvec(c, x, y, R, master, st);
+  } else {
+    CouplingLaunch L{};
+    L.pos = c->pos.ptr;
+    L.mofn = c->mofn.ptr;
+    L.coef = fp32 ? (const void *)c->coef32.ptr : (const void *)c->coef64.ptr;
+    L.pairs = fp32 ? c->pairs.ptr : nullptr;
+    L.n = c->n;
+    L.bs = c->bs;
+    L.n_int = c->n_int;
+    L.ncoef = c->ncoef;
+    L.rho_min = c->rho_min;
+    L.res = c->res;
+    L.x = x;
+    L.y = y;
+    L.nrhs = R;
+    L.master = master ? 1 : 0;
+    L.t = c->tmat.ptr;
+    L.ptype = c->ptype.ptr;
+    L.t_diag = c->t_diag;
+    const int ns = choose_split(c->n, R);
+    if (ns > 1) {
+      c->w_partial.reserve((size_t)ns * c->n * c->bs * R);
+      L.partial = c->w_partial.ptr;
+    }
+    c->launches += launch_coupling(L, fp32, ns, st);
+  }
   if (c->profiling) {
     SG_CUDA(cudaEventRecord(e1, st));
     c->events.push_back({e0, e1, fp32 ? 1 : 0});

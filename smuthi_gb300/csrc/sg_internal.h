@@ -92,6 +92,10 @@ int choose_split(int n_particles, int nrhs);
 void build_coefficients(int kind, const double2 *raw, int len_rho, int bs, double2 *coef64, float2 *coef32,
                         double2 *work, cudaStream_t st);
 int coef_count(int kind);
+// interval-bucketed FP32 operator (sg_bucket.cu)
+bool bucket_supported(const sg_context *c);
+void build_bucket_plan(sg_context *c, cudaStream_t st);
+int launch_bucket_matvec(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st);
 // FP32 per-pair data (interval index, t, cos, sin) for all ordered pairs.
 void build_pairs(const double2 *pos, int n, double rho_min, double res, int n_int, int4 *pairs, cudaStream_t st);
 
@@ -125,7 +129,21 @@ struct sg_context {
   sg::DevBuf<double2> coef64;
   sg::DevBuf<float2> coef32;
   sg::DevBuf<int4> pairs;
-  bool pairs_ready = false;
+  bool pairs_ready = false;  // FP32 operator data (bucket plan or pair table) is built
+
+  // interval-bucketed FP32 operator (sg_bucket.cu)
+  bool use_bucket = false;  // the bucket plan exists
+  // FP32 kernel autotuner: per RHS count, the faster of the per-receiver and the bucketed kernel
+  struct Tuned {
+    int nrhs, variant;  // 0 per-receiver, 1 bucketed
+    float ms_receiver, ms_bucket;
+  };
+  std::vector<Tuned> tuned;
+  int bk_T = 0, bk_tiles = 0, bk_S = 0;
+  sg::DevBuf<int> bk_members, bk_offs;
+  sg::DevBuf<int4> bk_rec;
+  sg::DevBuf<float2> bk_x32;
+  sg::DevBuf<double2> bk_yacc;
 
   // T-matrices
   int n_types = 0, t_diag = 1;
