@@ -37,6 +37,10 @@ extern "C" {
 /* arithmetic of an operator application */
 #define SG_FP64 0
 #define SG_FP32 1
+/* solver flag, OR-ed into sg_gmres_solve's precision with SG_FP32: the correction solves of the
+ * mixed form use one block Krylov space for all right-hand sides (block GMRES, restart <= 20)
+ * instead of independent lockstep Krylov spaces */
+#define SG_BLOCK_GMRES 2
 
 typedef struct sg_context sg_context;
 

@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, "libsmuthi_gb300.so")
 SG_OK, SG_ERR_ARG, SG_ERR_CUDA, SG_ERR_NOT_CONVERGED, SG_ERR_NAN, SG_ERR_NO_DEVICE = range(6)
 SG_LINEAR, SG_CUBIC, SG_CUBIC_HERMITE = 0, 1, 2
 SG_FP64, SG_FP32 = 0, 1
+SG_BLOCK_GMRES = 2  # OR-ed with SG_FP32: block GMRES correction solves
 KINDS = {"linear": SG_LINEAR, "cubic": SG_CUBIC, "cubic_hermite": SG_CUBIC_HERMITE}
 
 #: every entry point declared in include/smuthi_gb300.h

@@ -326,9 +326,10 @@ static int solve_dev_impl(sg_context *ctx, const double2 *b, double2 *x, int nrh
   SG_REQUIRE(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
   SG_REQUIRE(rtol > 0 && std::isfinite(rtol), "rtol must be positive");
   SG_REQUIRE(restart >= 0 && restart <= 128, "restart must be in [0, 128] (0 = 20)");
-  SG_REQUIRE(precision == SG_FP64 || precision == SG_FP32, "unknown precision");
+  SG_REQUIRE(precision == SG_FP64 || precision == SG_FP32 || precision == (SG_FP32 | SG_BLOCK_GMRES),
+             "unknown precision / solver flags");
   use_device(ctx);
-  if (precision == SG_FP32) ensure_pairs(ctx, st);
+  if (precision & SG_FP32) ensure_pairs(ctx, st);
   const size_t plen = ctx->padded(nrhs);
   const double2 *bp = b;
   double2 *xp = x;

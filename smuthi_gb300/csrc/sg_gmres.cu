@@ -207,6 +207,7 @@ struct GmresResult {
   int inner_iters = 0;
   int cycles = 0;
   int matvecs = 0;
+  bool breakdown = false;
   std::vector<double> relres;  // per rhs: final ||b - M x|| / ||b|| with the solve's operator
   std::vector<char> conv;
 };
@@ -461,9 +462,397 @@ static GmresResult gmres_lockstep(Solver &S, const double2 *b, double2 *x, doubl
   return res;
 }
 
+// ------------------------------------------------------------------ block GMRES
+// One block Krylov space for all active right-hand sides: block Arnoldi with classical Gram-Schmidt
+// applied twice, CholeskyQR2 for each new block, and the block-Hessenberg least-squares problem
+// solved by incrementally applied complex Householder reflectors on the host. Columns that already
+// meet the tolerance are compacted out at every restart.
+
+// partial[blk][i][a][b] = sum_{rows in blk} conj(V_i[row][a]) * W[row][b]   (16 x 16 (a, b) tiles)
+__global__ void gram_partial_kernel(VecList V, int nv, const double2 *W, size_t rows, int Ra, double2 *partial) {
+  __shared__ double2 vs[32][17], ws[32][17];
+  const int i = blockIdx.y;
+  const int ntile = (Ra + 15) / 16;
+  const int ta0 = (blockIdx.z / ntile) * 16, tb0 = (blockIdx.z % ntile) * 16;
+  const int tid = threadIdx.x, ta = tid / 16, tb = tid % 16;
+  const int a = ta0 + ta, b = tb0 + tb;
+  double sr = 0.0, si = 0.0;
+  const double2 *Vi = V.v[i];
+  for (size_t r0 = (size_t)blockIdx.x * 32; r0 < rows; r0 += (size_t)gridDim.x * 32) {
+    for (int e = tid; e < 32 * 16; e += blockDim.x) {
+      const int rr = e / 16, cc = e % 16;
+      const size_t row = r0 + rr;
+      const bool ok = row < rows;
+      vs[rr][cc] = (ok && ta0 + cc < Ra) ? Vi[row * Ra + ta0 + cc] : make_double2(0.0, 0.0);
+      ws[rr][cc] = (ok && tb0 + cc < Ra) ? W[row * Ra + tb0 + cc] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int rr = 0; rr < 32; ++rr) {
+      const double2 p = vs[rr][ta], q = ws[rr][tb];
+      sr = fma(p.x, q.x, fma(p.y, q.y, sr));
+      si = fma(p.x, q.y, fma(-p.y, q.x, si));
+    }
+    __syncthreads();
+  }
+  if (a < Ra && b < Ra) partial[(((size_t)blockIdx.x * nv + i) * Ra + a) * Ra + b] = make_double2(sr, si);
+}
+
+// out[e] = sum over blk of partial[blk][e], e < n
+__global__ void sum_partials_kernel(const double2 *partial, int nblk, size_t n, double2 *out) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  double sr = 0.0, si = 0.0;
+  for (int k = 0; k < nblk; ++k) {
+    const double2 v = partial[(size_t)k * n + e];
+    sr += v.x;
+    si += v.y;
+  }
+  out[e] = make_double2(sr, si);
+}
+
+// W[row][b] += sign * sum_i sum_a V_i[row][a] * C[i][a][b]; V blocks have Ra columns, W and C have Rc
+__global__ void block_combine_kernel(VecList V, int nv, int Ra, const double2 *C, int Rc, double sign, double2 *W,
+                                     size_t rows) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= rows * Rc) return;
+  const size_t row = e / Rc;
+  const int b = (int)(e - row * Rc);
+  double ar = 0.0, ai = 0.0;
+  for (int i = 0; i < nv; ++i) {
+    const double2 *vr = V.v[i] + row * Ra;
+    const double2 *ci = C + (size_t)i * Ra * Rc + b;
+    for (int a = 0; a < Ra; ++a) {
+      const double2 v = vr[a], h = ci[(size_t)a * Rc];
+      ar = fma(v.x, h.x, fma(-v.y, h.y, ar));
+      ai = fma(v.x, h.y, fma(v.y, h.x, ai));
+    }
+  }
+  W[e].x += sign * ar;
+  W[e].y += sign * ai;
+}
+
+// out[row][b] = sum_a W[row][a] * Mt[a][b]   (Ra x Ra)
+__global__ void right_mult_kernel(const double2 *W, const double2 *Mt, size_t rows, int Ra, double2 *out) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= rows * Ra) return;
+  const size_t row = e / Ra;
+  const int b = (int)(e - row * Ra);
+  double ar = 0.0, ai = 0.0;
+  for (int a = 0; a < Ra; ++a) {
+    const double2 w = W[row * Ra + a], m = Mt[(size_t)a * Ra + b];
+    ar = fma(w.x, m.x, fma(-w.y, m.y, ar));
+    ai = fma(w.x, m.y, fma(w.y, m.x, ai));
+  }
+  out[e] = make_double2(ar, ai);
+}
+
+// dst[row][q] = src[row][cols[q]] (gather) or dst[row][cols[q]] += src[row][q] (scatter-add)
+__global__ void cols_kernel(const double2 *src, double2 *dst, const int *cols, size_t rows, int Rwide, int Ra,
+                            int scatter_add) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= rows * Ra) return;
+  const size_t row = e / Ra;
+  const int q = (int)(e - row * Ra);
+  if (scatter_add) {
+    double2 &d = dst[row * Rwide + cols[q]];
+    d.x += src[e].x;
+    d.y += src[e].y;
+  } else {
+    dst[e] = src[row * Rwide + cols[q]];
+  }
+}
+
+struct BlockOps {
+  Solver &S;
+  sg_context *c;
+  size_t rows;
+  std::vector<cd> host;
+
+  // H[i] (Ra x Ra) = V_i^H W for i < nv, result on the host (row-major [i][a][b])
+  void gram(const VecList &V, int nv, const double2 *W, int Ra, std::vector<cd> &H) {
+    const int ntile = (Ra + 15) / 16;
+    const int nblk = (int)std::min<size_t>(152, (rows + 31) / 32);
+    const size_t n = (size_t)nv * Ra * Ra;
+    c->w_tmp.reserve((size_t)nblk * n + n);
+    dim3 grid(nblk, nv, ntile * ntile);
+    gram_partial_kernel<<<grid, 256, 0, S.st>>>(V, nv, W, rows, Ra, c->w_tmp.ptr);
+    SG_CUDA(cudaGetLastError());
+    double2 *out = c->w_tmp.ptr + (size_t)nblk * n;
+    sum_partials_kernel<<<nblocks(n), 256, 0, S.st>>>(c->w_tmp.ptr, nblk, n, out);
+    SG_CUDA(cudaGetLastError());
+    *S.launches += 2;
+    std::vector<double2> h(n);
+    SG_CUDA(cudaMemcpyAsync(h.data(), out, n * sizeof(double2), cudaMemcpyDeviceToHost, S.st));
+    SG_CUDA(cudaStreamSynchronize(S.st));
+    H.resize(n);
+    for (size_t e = 0; e < n; ++e) H[e] = cd(h[e].x, h[e].y);
+  }
+
+  // W += sign * sum_i V_i C_i with C on the host ([i][a][b], Ra x Rc blocks)
+  void combine(const VecList &V, int nv, int Ra, const std::vector<cd> &C, int Rc, double sign, double2 *W) {
+    std::vector<double2> h(C.size());
+    for (size_t e = 0; e < C.size(); ++e) h[e] = make_double2(C[e].real(), C[e].imag());
+    c->w_hcol.reserve(std::max<size_t>(c->w_hcol.n, h.size()));
+    SG_CUDA(cudaMemcpyAsync(c->w_hcol.ptr, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice, S.st));
+    block_combine_kernel<<<nblocks(rows * Rc), 256, 0, S.st>>>(V, nv, Ra, c->w_hcol.ptr, Rc, sign, W, rows);
+    SG_CUDA(cudaGetLastError());
+    *S.launches += 1;
+  }
+
+  // CholeskyQR2: W (rows x Ra) -> orthonormal Q in place, Rf (Ra x Ra upper, row-major). false on breakdown.
+  bool cholqr2(double2 *W, double2 *tmp, int Ra, std::vector<cd> &Rf) {
+    std::vector<cd> Rtot(Ra * Ra, 0.0);
+    for (int a = 0; a < Ra; ++a) Rtot[a * Ra + a] = 1.0;
+    for (int pass = 0; pass < 2; ++pass) {
+      VecList L{};
+      L.v[0] = W;
+      std::vector<cd> G;
+      gram(L, 1, W, Ra, G);
+      // Cholesky G = U^H U (U upper)
+      std::vector<cd> U(Ra * Ra, 0.0);
+      double gmax = 0.0;
+      for (int a = 0; a < Ra; ++a) gmax = std::max(gmax, G[a * Ra + a].real());
+      for (int a = 0; a < Ra; ++a) {
+        cd d = G[a * Ra + a];
+        for (int k = 0; k < a; ++k) d -= std::conj(U[k * Ra + a]) * U[k * Ra + a];
+        if (!(d.real() > 1e-24 * std::max(gmax, 1e-300))) return false;
+        const double ua = std::sqrt(d.real());
+        U[a * Ra + a] = ua;
+        for (int b = a + 1; b < Ra; ++b) {
+          cd v = G[a * Ra + b];
+          for (int k = 0; k < a; ++k) v -= std::conj(U[k * Ra + a]) * U[k * Ra + b];
+          U[a * Ra + b] = v / ua;
+        }
+      }
+      // Uinv (upper) by back substitution
+      std::vector<cd> Ui(Ra * Ra, 0.0);
+      for (int col = 0; col < Ra; ++col) {
+        for (int a = Ra - 1; a >= 0; --a) {
+          cd v = (a == col) ? cd(1.0) : cd(0.0);
+          for (int k = a + 1; k < Ra; ++k) v -= U[a * Ra + k] * Ui[k * Ra + col];
+          Ui[a * Ra + col] = v / U[a * Ra + a];
+        }
+      }
+      std::vector<double2> h(Ra * Ra);
+      for (int e = 0; e < Ra * Ra; ++e) h[e] = make_double2(Ui[e].real(), Ui[e].imag());
+      c->w_red.reserve(std::max<size_t>(c->w_red.n, 2 * (size_t)Ra * Ra));
+      double2 *dm = reinterpret_cast<double2 *>(c->w_red.ptr);
+      SG_CUDA(cudaMemcpyAsync(dm, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice, S.st));
+      right_mult_kernel<<<nblocks(rows * Ra), 256, 0, S.st>>>(W, dm, rows, Ra, tmp);
+      SG_CUDA(cudaGetLastError());
+      SG_CUDA(cudaMemcpyAsync(W, tmp, rows * Ra * sizeof(double2), cudaMemcpyDeviceToDevice, S.st));
+      *S.launches += 1;
+      SG_CUDA(cudaStreamSynchronize(S.st));
+      // Rtot = U * Rtot
+      std::vector<cd> Rn(Ra * Ra, 0.0);
+      for (int a = 0; a < Ra; ++a)
+        for (int b = 0; b < Ra; ++b) {
+          cd v = 0.0;
+          for (int k = a; k < Ra; ++k) v += U[a * Ra + k] * Rtot[k * Ra + b];
+          Rn[a * Ra + b] = v;
+        }
+      Rtot.swap(Rn);
+    }
+    Rf.swap(Rtot);
+    return true;
+  }
+};
+
+// Complex Householder reflector for x (length len): returns v (v[0] set) and beta; H x = beta e1,
+// H = I - 2 v v^H / (v^H v).
+static void householder(cd *x, int len, std::vector<cd> &v, cd &beta) {
+  double nrm = 0.0;
+  for (int k = 0; k < len; ++k) nrm += std::norm(x[k]);
+  nrm = std::sqrt(nrm);
+  v.assign(x, x + len);
+  if (nrm == 0.0) {
+    beta = 0.0;
+    return;
+  }
+  const double ax = std::abs(x[0]);
+  const cd ph = ax > 0 ? x[0] / ax : cd(1.0);
+  beta = -ph * nrm;
+  v[0] = x[0] - beta;
+}
+
+static void apply_reflector(const std::vector<cd> &v, cd *y, int len) {
+  cd vh_y = 0.0;
+  double vv = 0.0;
+  for (int k = 0; k < len; ++k) {
+    vh_y += std::conj(v[k]) * y[k];
+    vv += std::norm(v[k]);
+  }
+  if (vv == 0.0) return;
+  const cd f = 2.0 * vh_y / vv;
+  for (int k = 0; k < len; ++k) y[k] -= f * v[k];
+}
+
+// Block GMRES on padded device vectors (nrhs = S.R); x holds x0 (zero_x0: x0 == 0). Returns the
+// per-RHS explicit residual of the final iterate with the solve's operator.
+static GmresResult block_gmres(Solver &S, const double2 *b, double2 *x, double rtol, int restart, int max_cycles,
+                               bool fp32, bool zero_x0, const std::vector<char> &skip) {
+  sg_context *c = S.c;
+  const int R = S.R;
+  const size_t rows = S.rows, len = S.len();
+  restart = std::max(1, std::min(restart, 20));
+  BlockOps ops{S, c, rows, {}};
+  GmresResult res;
+  res.relres.assign(R, 0.0);
+  res.conv.assign(R, 0);
+  c->w_basis.reserve((size_t)(restart + 1) * len);
+  c->w_w.reserve(len);
+  c->w_r.reserve(len);
+  c->w_d.reserve(len);
+  c->w_b.reserve(std::max<size_t>(c->w_b.n, len));
+  double2 *r = c->w_r.ptr, *W = c->w_w.ptr, *tmp = c->w_d.ptr;
+  std::vector<double2> hb((size_t)kHcol * R);
+  auto col_norms = [&](const double2 *v, std::vector<double> &out) {
+    VecList L{};
+    L.v[0] = v;
+    S.dots(L, 1, v, c->w_hcol.ptr);
+    SG_CUDA(cudaMemcpyAsync(hb.data(), c->w_hcol.ptr, R * sizeof(double2), cudaMemcpyDeviceToHost, S.st));
+    SG_CUDA(cudaStreamSynchronize(S.st));
+    out.resize(R);
+    for (int q = 0; q < R; ++q) out[q] = std::sqrt(std::max(0.0, hb[q].x));
+  };
+  c->w_hcol.reserve((size_t)kHcol * R);
+  std::vector<double> bnrm, rn;
+  col_norms(b, bnrm);
+  if (zero_x0) {
+    SG_CUDA(cudaMemcpyAsync(r, b, len * sizeof(double2), cudaMemcpyDeviceToDevice, S.st));
+  } else {
+    S.master(x, r, fp32);
+    res.matvecs++;
+    sub_from_kernel<<<nblocks(len), 256, 0, S.st>>>(b, r, len);
+    SG_CUDA(cudaGetLastError());
+  }
+  DevBuf<int> dcols;
+  dcols.reserve(R);
+  for (int cycle = 0; cycle < max_cycles; ++cycle) {
+    col_norms(r, rn);
+    std::vector<int> cols;
+    for (int q = 0; q < R; ++q) {
+      if (bnrm[q] > 0) res.relres[q] = rn[q] / bnrm[q];
+      const bool ok = rn[q] <= rtol * bnrm[q] || bnrm[q] == 0.0;
+      res.conv[q] = ok ? 1 : 0;
+      if (!ok && (skip.empty() || !skip[q])) cols.push_back(q);
+    }
+    if (cols.empty()) break;
+    res.cycles++;
+    const int Ra = (int)cols.size();
+    const size_t blen = rows * Ra;
+    auto Vk = [&](int k) { return c->w_basis.ptr + (size_t)k * blen; };
+    SG_CUDA(cudaMemcpyAsync(dcols.ptr, cols.data(), Ra * sizeof(int), cudaMemcpyHostToDevice, S.st));
+    cols_kernel<<<nblocks(blen), 256, 0, S.st>>>(r, Vk(0), dcols.ptr, rows, R, Ra, 0);
+    SG_CUDA(cudaGetLastError());
+    std::vector<cd> beta;
+    if (!ops.cholqr2(Vk(0), tmp, Ra, beta)) {
+      res.breakdown = true;
+      break;
+    }
+    // G = Q^H E1 beta, Rfac = triangular factor, reflectors per column
+    const int maxrow = (restart + 1) * Ra;
+    std::vector<cd> G((size_t)maxrow * Ra, 0.0);  // row-major [row][q]
+    for (int a = 0; a < Ra; ++a)
+      for (int q = 0; q < Ra; ++q) G[(size_t)a * Ra + q] = beta[a * Ra + q];
+    std::vector<std::vector<cd>> refl;                    // reflector for column c acts on rows c..c+Ra
+    std::vector<cd> Rcol((size_t)restart * Ra * maxrow);  // column-major columns of the triangular factor
+    int jdone = 0;
+    bool stop = false;
+    for (int j = 0; j < restart && !stop; ++j) {
+      // W = M V_j on the compacted block
+      S.R = Ra;
+      S.master(Vk(j), W, fp32);
+      S.R = R;
+      res.matvecs++;
+      VecList L{};
+      for (int k = 0; k <= j; ++k) L.v[k] = Vk(k);
+      std::vector<cd> H1, H2;
+      ops.gram(L, j + 1, W, Ra, H1);
+      ops.combine(L, j + 1, Ra, H1, Ra, -1.0, W);
+      ops.gram(L, j + 1, W, Ra, H2);
+      ops.combine(L, j + 1, Ra, H2, Ra, -1.0, W);
+      for (size_t e = 0; e < H1.size(); ++e) H1[e] += H2[e];
+      std::vector<cd> Hs;
+      const bool ok = ops.cholqr2(W, tmp, Ra, Hs);
+      if (ok) SG_CUDA(cudaMemcpyAsync(Vk(j + 1), W, blen * sizeof(double2), cudaMemcpyDeviceToDevice, S.st));
+      // new block column: rows 0 .. (j+2)Ra
+      const int nr = (j + 2) * Ra;
+      for (int cc = 0; cc < Ra; ++cc) {
+        cd *col = &Rcol[(size_t)(j * Ra + cc) * maxrow];
+        for (int rr = 0; rr < maxrow; ++rr) col[rr] = 0.0;
+        for (int i = 0; i <= j; ++i)
+          for (int a = 0; a < Ra; ++a) col[i * Ra + a] = H1[((size_t)i * Ra + a) * Ra + cc];
+        for (int a = 0; a < Ra; ++a) col[(j + 1) * Ra + a] = ok ? Hs[a * Ra + cc] : cd(0.0);
+        // previous reflectors
+        for (size_t k = 0; k < refl.size(); ++k) apply_reflector(refl[k], col + k, (int)refl[k].size());
+      }
+      // new reflectors for columns j*Ra .. (j+1)*Ra-1
+      for (int cc = 0; cc < Ra; ++cc) {
+        const int cidx = j * Ra + cc;
+        cd *col = &Rcol[(size_t)cidx * maxrow];
+        const int l = std::min(Ra + 1, nr - cidx);
+        std::vector<cd> v;
+        cd bet;
+        householder(col + cidx, l, v, bet);
+        col[cidx] = bet;
+        for (int k = 1; k < l; ++k) col[cidx + k] = 0.0;
+        for (int c2 = cc + 1; c2 < Ra; ++c2) apply_reflector(v, &Rcol[(size_t)(j * Ra + c2) * maxrow] + cidx, l);
+        // apply to G columns
+        for (int q = 0; q < Ra; ++q) {
+          std::vector<cd> g(l);
+          for (int k = 0; k < l; ++k) g[k] = G[(size_t)(cidx + k) * Ra + q];
+          apply_reflector(v, g.data(), l);
+          for (int k = 0; k < l; ++k) G[(size_t)(cidx + k) * Ra + q] = g[k];
+        }
+        refl.push_back(v);
+      }
+      jdone = j + 1;
+      res.inner_iters++;
+      // implicit residual per active column: rows (j+1)Ra .. (j+2)Ra of G
+      bool all = true;
+      for (int q = 0; q < Ra; ++q) {
+        double s2 = 0.0;
+        for (int a = 0; a < Ra; ++a) s2 += std::norm(G[(size_t)((j + 1) * Ra + a) * Ra + q]);
+        if (std::sqrt(s2) > rtol * bnrm[cols[q]]) all = false;
+      }
+      if (all || !ok) stop = true;
+    }
+    // Y = Rfac^{-1} G[0 : jdone*Ra]
+    const int K = jdone * Ra;
+    std::vector<cd> Y((size_t)K * Ra, 0.0);
+    for (int q = 0; q < Ra; ++q)
+      for (int rr = K - 1; rr >= 0; --rr) {
+        cd v = G[(size_t)rr * Ra + q];
+        for (int k = rr + 1; k < K; ++k) v -= Rcol[(size_t)k * maxrow + rr] * Y[(size_t)k * Ra + q];
+        const cd d = Rcol[(size_t)rr * maxrow + rr];
+        Y[(size_t)rr * Ra + q] = d != 0.0 ? v / d : cd(0.0);
+      }
+    // dx = V Y (compact), x[:, cols] += dx
+    VecList L{};
+    for (int k = 0; k < jdone; ++k) L.v[k] = Vk(k);
+    k_zero(tmp, blen, S.st);
+    ops.combine(L, jdone, Ra, Y, Ra, 1.0, tmp);
+    cols_kernel<<<nblocks(blen), 256, 0, S.st>>>(tmp, x, dcols.ptr, rows, R, Ra, 1);
+    SG_CUDA(cudaGetLastError());
+    // explicit residual
+    S.master(x, r, fp32);
+    res.matvecs++;
+    sub_from_kernel<<<nblocks(len), 256, 0, S.st>>>(b, r, len);
+    SG_CUDA(cudaGetLastError());
+  }
+  col_norms(r, rn);
+  for (int q = 0; q < R; ++q) {
+    if (bnrm[q] > 0) res.relres[q] = rn[q] / bnrm[q];
+    res.conv[q] = (rn[q] <= rtol * bnrm[q] || bnrm[q] == 0.0) ? 1 : 0;
+  }
+  return res;
+}
+
 // Mixed precision: FP32-operator GMRES corrections inside FP64 iterative refinement.
 static GmresResult refine_mixed(Solver &S, const double2 *b, double2 *x, double rtol, int restart, int maxiter,
-                                int &fp64_mv, int &fp32_mv, int &steps) {
+                                int &fp64_mv, int &fp32_mv, int &steps, bool block) {
   sg_context *c = S.c;
   const int R = S.R;
   const size_t len = S.len();
@@ -533,7 +922,17 @@ static GmresResult refine_mixed(Solver &S, const double2 *b, double2 *x, double 
     tau = std::max(1e-6, std::min(0.5, tau));
     k_zero(d, len, S.st);
     const int cycles = std::max(1, std::min(inner_cap_cycles, (maxiter - inner_total) / restart + 1));
-    GmresResult g = gmres_lockstep(S, rr, d, tau, restart, cycles, true, true, done, 2);
+    GmresResult g;
+    bool use_block = block && R > 1;
+    if (use_block) {
+      const int brestart = std::min(restart, 20);
+      g = block_gmres(S, rr, d, tau, brestart, std::max(1, std::min(inner_cap_cycles, 200)), true, true, done);
+      if (g.breakdown && g.inner_iters == 0) {
+        k_zero(d, len, S.st);
+        use_block = false;
+      }
+    }
+    if (!use_block) g = gmres_lockstep(S, rr, d, tau, restart, cycles, true, true, done, 2);
     fp32_mv += g.matvecs;
     inner_total += g.inner_iters;
     out.inner_iters += g.inner_iters;
@@ -561,8 +960,9 @@ void solve_padded(sg_context *c, const double2 *b, double2 *x, int R, double rto
   SG_CUDA(cudaEventRecord(ev0, st));
   GmresResult g;
   int fp64_mv = 0, fp32_mv = 0, steps = 0;
-  if (precision == SG_FP32) {
-    g = refine_mixed(S, b, x, rtol, restart, maxiter * restart, fp64_mv, fp32_mv, steps);
+  if (precision & SG_FP32) {
+    g = refine_mixed(S, b, x, rtol, restart, maxiter * restart, fp64_mv, fp32_mv, steps,
+                     (precision & SG_BLOCK_GMRES) != 0);
   } else {
     g = gmres_lockstep(S, b, x, rtol, restart, maxiter, false, false, std::vector<char>());
     fp64_mv = g.matvecs;

@@ -214,3 +214,25 @@ def test_full_size_c2_properties(gpu_context):
     y2 = gpu_context.coupling_matvec(x2, 0)
     y12 = gpu_context.coupling_matvec(x + 0.5j * x2, 0)
     assert gc.relerr(y12, y + 0.5j * y2) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["c5s", "c1"])
+def test_block_gmres_mixed(name, gpu_context):
+    """Block GMRES correction solves (one Krylov space for all RHS) reach the FP64-true tolerance."""
+    from smuthi_gb300 import _lib
+    g = gc.load(name)
+    kind = _kinds(g)[0]
+    parts, ls, wl, W, M = _product_system(g, kind, gpu_context)
+    keys = sorted(k for k in g if k.startswith("rhs_"))
+    rng = np.random.default_rng(2)
+    cols = [g[k] for k in keys]
+    while len(cols) < 3:  # extra right-hand sides: perturbed copies (not collinear)
+        cols.append(cols[0] * (1 + 0.3 * rng.standard_normal(len(cols[0]))))
+    B = np.ascontiguousarray(np.stack(cols, axis=1))
+    X, info = gpu_context.gmres(B, np.zeros_like(B), 1e-6, restart=20, precision=_lib.SG_FP32 | _lib.SG_BLOCK_GMRES)
+    assert info.converged == B.shape[1]
+    assert gpu_context.true_residual(B, X).max() <= 1e-6
+    for q, k in enumerate(keys):
+        bk = "b_" + k[4:]
+        if bk in g:
+            assert gc.relerr(X[:, q], g[bk]) < 1e-4
