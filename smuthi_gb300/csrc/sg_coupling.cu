@@ -149,7 +149,10 @@ __global__ void __launch_bounds__(kThreads) coupling_kernel(const CouplingLaunch
           cplx u;
           u.x = ph_re[q] * xr - ph_im[q] * xim;
           u.y = ph_re[q] * xim + ph_im[q] * xr;
-          ubuf[r * bs + nrow[q]] = u;  // [r][n2]: lane-consecutive writes
+          // FP64: [r][n2] (lane-consecutive writes); FP32: [n2][r] (the n2 loop reads the RHS tile
+          // with vector loads, which matters more than the write conflicts)
+          if (sizeof(Real) == sizeof(double)) ubuf[r * bs + nrow[q]] = u;
+          else ubuf[nrow[q] * RT + r] = u;
         }
       }
     }
@@ -163,7 +166,7 @@ __global__ void __launch_bounds__(kThreads) coupling_kernel(const CouplingLaunch
     for (int n2 = 0; n2 < bs; ++n2) {
       cplx u[RT];
 #pragma unroll
-      for (int r = 0; r < RT; ++r) u[r] = ubuf[r * bs + n2];
+      for (int r = 0; r < RT; ++r) u[r] = (sizeof(Real) == sizeof(double)) ? ubuf[r * bs + n2] : ubuf[n2 * RT + r];
 #pragma unroll
       for (int q = 0; q < P; ++q) {
         const cplx *cp = cbase + (size_t)n2 * bs + nrowc[q];
