@@ -41,6 +41,10 @@ extern "C" {
  * mixed form use one block Krylov space for all right-hand sides (block GMRES, restart <= 20)
  * instead of independent lockstep Krylov spaces */
 #define SG_BLOCK_GMRES 2
+/* solver flag, OR-ed into sg_gmres_solve's precision with SG_FP32: the correction solves are
+ * right-preconditioned flexible GMRES with the learned preconditioner selected by
+ * sg_precond_select; a correction solve that fails to reduce its residual is redone without it */
+#define SG_PRECOND 4
 
 typedef struct sg_context sg_context;
 
@@ -99,7 +103,7 @@ typedef struct sg_solve_info {
   int32_t fp64_matvecs;    /* FP64 operator applications */
   int32_t fp32_matvecs;    /* FP32 operator applications */
   int32_t converged;       /* number of rhs that met the tolerance */
-  int32_t reserved;
+  int32_t precond_fallbacks; /* SG_PRECOND: correction solves redone without the preconditioner */
   double max_rel_residual; /* max over rhs of ||b - M x|| / ||b|| (FP64 operator) */
   double seconds;          /* host wall time of the solve call */
   double device_seconds;   /* CUDA-event time of the solve on the context's stream */
@@ -159,6 +163,38 @@ int sg_measure_fma_peak(sg_context *ctx, int precision, double *tflops);
 int sg_coupling_matvec_linear_noalloc(int device, int n_particles, const void *xy, int blocksize,
                                       const void *m_of_n, int len_rho, double rho_min, double resolution,
                                       const void *table, const void *x, void *y, int nrhs, void *stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Learned preconditioner for the mixed solve (no counterpart in the reference, whose GMRES call
+ * at smuthi/linearsystem/linear_system.py:285 is unpreconditioned). A message-passing network on
+ * the k-nearest-neighbour graph of the particles: three layers, each a near-field coupling
+ * a = sum_s T_i W_{i,nbr(i,s)} h followed by an MLP (4*blocksize -> 128 -> 2*blocksize, BF16
+ * weights, FP32 accumulation), h <- u + alpha a + MLP([a, h]) with u the normalised input. With
+ * zero output weights and alpha = 1 it is the Neumann series (I - T W_near)^{-1} ~ I + A + A^2 + A^3.
+ * It needs diagonal T-matrices (sg_set_tmatrix, diagonal = 1), uniform blocks and blocksize <= 64.
+ * Parameters are one flat float32 vector of sg_precond_param_count(blocksize) entries; per layer
+ * W1[128][4B], b1[128], W2[2B][128], b2[2B], alpha[2] (B = blocksize). */
+int sg_precond_param_count(int blocksize);
+
+/* Add a graph for the current particles: nbr[i*(k+1) + s], slot 0 = i itself, then k neighbours.
+ * Builds the near-field blocks from the lookup coefficients (sg_set_lookup first). Returns its id. */
+int sg_precond_add_graph(sg_context *ctx, int k, const int32_t *nbr, int *graph_id);
+/* Select the graph used by SG_PRECOND solves and sg_precond_apply_dev (-1 = none). */
+int sg_precond_select(sg_context *ctx, int graph_id);
+/* Drop every graph (the particle set changed). */
+int sg_precond_clear(sg_context *ctx);
+int sg_precond_set_params(sg_context *ctx, int blocksize, const float *params, int count);
+int sg_precond_get_params(sg_context *ctx, float *params, int count);
+/* z = P v for nvec <= 64 vectors (device buffers, reference layout n_unknowns x nvec). */
+int sg_precond_apply_dev(sg_context *ctx, const void *v, void *z, int nvec, void *stream);
+/* One training step on graph graph_id with nvec <= 64 pairs (v, e = M^{-1} v) (device buffers,
+ * reference layout): loss = mean_q ||P(v_q)/|v_q| - e_q/|v_q|||^2 / ||e_q/|v_q|||^2. Writes the loss,
+ * the gradient (if grad != NULL, param_count floats) and, when lr > 0, takes an Adam step
+ * (beta1 0.9, beta2 0.999, eps 1e-8; step = 1, 2, ... for the bias corrections). Synchronous. */
+int sg_precond_train_step(sg_context *ctx, int graph_id, const void *v, const void *e, int nvec, float lr,
+                          int step, double *loss, float *grad);
+/* Copy a graph's near-field blocks (complex64 [n][k+1][B][B], n2 fastest) to the host. */
+int sg_precond_export_blocks(sg_context *ctx, int graph_id, float *blocks);
 
 #ifdef __cplusplus
 }

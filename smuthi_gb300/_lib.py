@@ -18,6 +18,7 @@ SG_OK, SG_ERR_ARG, SG_ERR_CUDA, SG_ERR_NOT_CONVERGED, SG_ERR_NAN, SG_ERR_NO_DEVI
 SG_LINEAR, SG_CUBIC, SG_CUBIC_HERMITE = 0, 1, 2
 SG_FP64, SG_FP32 = 0, 1
 SG_BLOCK_GMRES = 2  # OR-ed with SG_FP32: block GMRES correction solves
+SG_PRECOND = 4  # OR-ed with SG_FP32: flexible GMRES corrections with the learned preconditioner
 KINDS = {"linear": SG_LINEAR, "cubic": SG_CUBIC, "cubic_hermite": SG_CUBIC_HERMITE}
 
 #: every entry point declared in include/smuthi_gb300.h
@@ -25,7 +26,9 @@ EXPORTS = ("sg_last_error", "sg_version", "sg_create", "sg_destroy", "sg_set_par
            "sg_set_tmatrix", "sg_coupling_matvec", "sg_master_matvec", "sg_coupling_matvec_dev",
            "sg_master_matvec_dev", "sg_gmres_solve", "sg_gmres_solve_dev", "sg_true_residual", "sg_profile",
            "sg_kernel_timing", "sg_launch_count", "sg_measure_fma_peak", "sg_fp32_autotune",
-           "sg_coupling_matvec_linear_noalloc")
+           "sg_coupling_matvec_linear_noalloc", "sg_precond_param_count", "sg_precond_add_graph",
+           "sg_precond_select", "sg_precond_clear", "sg_precond_set_params", "sg_precond_get_params",
+           "sg_precond_apply_dev", "sg_precond_train_step", "sg_precond_export_blocks")
 
 
 class LibraryMissing(RuntimeError):
@@ -44,12 +47,13 @@ class NotConverged(SmuthiGB300Error):
 
 class SolveInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("restarts", ctypes.c_int32), ("fp64_matvecs", ctypes.c_int32),
-                ("fp32_matvecs", ctypes.c_int32), ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("fp32_matvecs", ctypes.c_int32), ("converged", ctypes.c_int32),
+                ("precond_fallbacks", ctypes.c_int32),
                 ("max_rel_residual", ctypes.c_double), ("seconds", ctypes.c_double),
                 ("device_seconds", ctypes.c_double)]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 _LIB = None
@@ -80,6 +84,15 @@ def _declare(L):
         "sg_measure_fma_peak": [_P, _I, ctypes.POINTER(_D)],
         "sg_fp32_autotune": [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D)],
         "sg_coupling_matvec_linear_noalloc": [_I, _I, _P, _I, _P, _I, _D, _D, _P, _P, _P, _I, _P],
+        "sg_precond_param_count": [_I],
+        "sg_precond_add_graph": [_P, _I, _P, ctypes.POINTER(_I)],
+        "sg_precond_select": [_P, _I],
+        "sg_precond_clear": [_P],
+        "sg_precond_set_params": [_P, _I, _P, _I],
+        "sg_precond_get_params": [_P, _P, _I],
+        "sg_precond_apply_dev": [_P, _P, _P, _I, _P],
+        "sg_precond_train_step": [_P, _I, _P, _P, _I, ctypes.c_float, _I, ctypes.POINTER(_D), _P],
+        "sg_precond_export_blocks": [_P, _I, _P],
     }
     for name, args in sigs.items():
         fn = getattr(L, name)
@@ -227,6 +240,46 @@ class Context:
         b = ctypes.c_double()
         check(lib().sg_fp32_autotune(self.h, int(nrhs), ctypes.byref(v), ctypes.byref(a), ctypes.byref(b)))
         return v.value, a.value, b.value
+
+    # -- learned preconditioner
+    def precond_add_graph(self, nbr):
+        """Upload a neighbour table nbr[n][k+1] (slot 0 = the particle itself); returns its graph id."""
+        nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+        gid = ctypes.c_int()
+        check(lib().sg_precond_add_graph(self.h, nbr.shape[1] - 1, ptr(nbr), ctypes.byref(gid)))
+        return gid.value
+
+    def precond_select(self, graph_id):
+        check(lib().sg_precond_select(self.h, int(graph_id)))
+
+    def precond_clear(self):
+        check(lib().sg_precond_clear(self.h))
+
+    def precond_set_params(self, blocksize, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        check(lib().sg_precond_set_params(self.h, int(blocksize), ptr(p), p.size))
+
+    def precond_get_params(self, count):
+        p = np.zeros(count, np.float32)
+        check(lib().sg_precond_get_params(self.h, ptr(p), count))
+        return p
+
+    def precond_apply_dev(self, v_ptr, z_ptr, nvec, stream=None):
+        check(lib().sg_precond_apply_dev(self.h, ctypes.c_void_p(v_ptr), ctypes.c_void_p(z_ptr), int(nvec),
+                                         ctypes.c_void_p(stream or 0)))
+
+    def precond_train_step(self, graph_id, v_ptr, e_ptr, nvec, lr=0.0, step=0, grad=None):
+        """Loss of one batch (and the gradient into ``grad`` when given); an Adam step when lr > 0."""
+        loss = ctypes.c_double()
+        gp = ptr(grad) if grad is not None else None
+        check(lib().sg_precond_train_step(self.h, int(graph_id), ctypes.c_void_p(v_ptr), ctypes.c_void_p(e_ptr),
+                                          int(nvec), float(lr), int(step), ctypes.byref(loss), gp))
+        return loss.value
+
+    def precond_export_blocks(self, graph_id, n, k1, bs):
+        out = np.zeros((n, k1, bs, bs), np.complex64)
+        check(lib().sg_precond_export_blocks(self.h, int(graph_id), ptr(out)))
+        return out
 
     def launch_count(self):
         n = ctypes.c_int64()

@@ -155,6 +155,8 @@ int sg_set_particles(sg_context *ctx, int n_particles, const double *xy, int n_u
     ctx->pairs_ready = false;
     ctx->kind = -1;  // the table must be re-uploaded for a new geometry
     ctx->t_ready = false;
+    ctx->pgraphs.clear();  // preconditioner graphs belong to the old particles
+    ctx->p_active = -1;
     return SG_OK;
   });
 }
@@ -202,6 +204,8 @@ int sg_set_lookup(sg_context *ctx, int kind, int len_rho, double rho_min, double
     ctx->rho_min = rho_min;
     ctx->res = resolution;
     ctx->pairs_ready = false;
+    ctx->pgraphs.clear();  // their near-field blocks came from the old table
+    ctx->p_active = -1;
     return SG_OK;
   });
 }
@@ -240,6 +244,8 @@ int sg_set_tmatrix(sg_context *ctx, int n_types, const double *t, const int32_t 
     ctx->n_types = n_types;
     ctx->t_diag = diagonal ? 1 : 0;
     ctx->t_ready = true;
+    ctx->pgraphs.clear();  // their near-field blocks hold the old T-matrices
+    ctx->p_active = -1;
     return SG_OK;
   });
 }
@@ -326,8 +332,14 @@ static int solve_dev_impl(sg_context *ctx, const double2 *b, double2 *x, int nrh
   SG_REQUIRE(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
   SG_REQUIRE(rtol > 0 && std::isfinite(rtol), "rtol must be positive");
   SG_REQUIRE(restart >= 0 && restart <= 128, "restart must be in [0, 128] (0 = 20)");
-  SG_REQUIRE(precision == SG_FP64 || precision == SG_FP32 || precision == (SG_FP32 | SG_BLOCK_GMRES),
+  SG_REQUIRE(precision == SG_FP64 || precision == SG_FP32 || precision == (SG_FP32 | SG_BLOCK_GMRES) ||
+                 precision == (SG_FP32 | SG_PRECOND),
              "unknown precision / solver flags");
+  if (precision & SG_PRECOND) {
+    SG_REQUIRE(ctx->p_active >= 0, "SG_PRECOND needs a preconditioner graph (sg_precond_select)");
+    SG_REQUIRE(ctx->p_count == sg::precond_param_count(ctx->bs), "SG_PRECOND needs parameters (sg_precond_set_params)");
+    SG_REQUIRE(nrhs <= 64, "SG_PRECOND handles at most 64 right-hand sides per solve");
+  }
   use_device(ctx);
   if (precision & SG_FP32) ensure_pairs(ctx, st);
   const size_t plen = ctx->padded(nrhs);
@@ -471,6 +483,96 @@ int sg_fp32_autotune(sg_context *ctx, int nrhs, int *variant, double *ms_receive
         return SG_OK;
       }
     *variant = -1;
+    return SG_OK;
+  });
+}
+
+int sg_precond_param_count(int blocksize) {
+  if (blocksize < 1 || blocksize > 64) return -1;
+  return sg::precond_param_count(blocksize);
+}
+
+int sg_precond_add_graph(sg_context *ctx, int k, const int32_t *nbr, int *graph_id) {
+  return guarded([&]() -> int {
+    require_ready(ctx, true);
+    SG_REQUIRE(nbr && graph_id, "null argument");
+    use_device(ctx);
+    sg::precond_add_graph(ctx, k, nbr, graph_id, ctx->stream);
+    return SG_OK;
+  });
+}
+
+int sg_precond_select(sg_context *ctx, int graph_id) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx != nullptr, "null context");
+    SG_REQUIRE(graph_id >= -1 && graph_id < (int)ctx->pgraphs.size(), "bad preconditioner graph id");
+    ctx->p_active = graph_id;
+    return SG_OK;
+  });
+}
+
+int sg_precond_clear(sg_context *ctx) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx != nullptr, "null context");
+    use_device(ctx);
+    SG_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->pgraphs.clear();
+    ctx->p_active = -1;
+    return SG_OK;
+  });
+}
+
+int sg_precond_set_params(sg_context *ctx, int blocksize, const float *params, int count) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx && params, "null argument");
+    for (int i = 0; i < count; ++i) SG_REQUIRE(std::isfinite(params[i]), "parameters hold NaN or Inf");
+    use_device(ctx);
+    sg::precond_set_params(ctx, blocksize, params, count, ctx->stream);
+    return SG_OK;
+  });
+}
+
+int sg_precond_get_params(sg_context *ctx, float *params, int count) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx && params, "null argument");
+    use_device(ctx);
+    sg::precond_get_params(ctx, params, count, ctx->stream);
+    return SG_OK;
+  });
+}
+
+int sg_precond_apply_dev(sg_context *ctx, const void *v, void *z, int nvec, void *stream) {
+  return guarded([&]() -> int {
+    require_ready(ctx, true);
+    SG_REQUIRE(v && z, "null vector");
+    SG_REQUIRE(ctx->uniform, "the learned preconditioner works on uniform particle blocks");
+    use_device(ctx);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    sg::precond_apply(ctx, (const double2 *)v, (double2 *)z, nvec, st);
+    return SG_OK;
+  });
+}
+
+int sg_precond_train_step(sg_context *ctx, int graph_id, const void *v, const void *e, int nvec, float lr, int step,
+                          double *loss, float *grad) {
+  return guarded([&]() -> int {
+    require_ready(ctx, true);
+    SG_REQUIRE(v && e, "null vector");
+    SG_REQUIRE(ctx->uniform, "the learned preconditioner works on uniform particle blocks");
+    SG_REQUIRE(lr >= 0.f && std::isfinite(lr), "lr must be >= 0");
+    SG_REQUIRE(lr == 0.f || step >= 1, "step must be >= 1 for an Adam update");
+    use_device(ctx);
+    sg::precond_train(ctx, graph_id, (const double2 *)v, (const double2 *)e, nvec, lr, step, loss, grad,
+                      ctx->stream);
+    return SG_OK;
+  });
+}
+
+int sg_precond_export_blocks(sg_context *ctx, int graph_id, float *blocks) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx && blocks, "null argument");
+    use_device(ctx);
+    sg::precond_export_blocks(ctx, graph_id, blocks, ctx->stream);
     return SG_OK;
   });
 }

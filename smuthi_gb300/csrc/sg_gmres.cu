@@ -216,13 +216,18 @@ struct GmresResult {
 // stall_cycles > 0 stops a right-hand side whose explicit residual fell by less than 5% over that many
 // consecutive restart cycles (used for the FP32-operator correction solves, whose residual has a noise
 // floor near the FP32 operator error); 0 keeps scipy's semantics.
+// precond = true runs flexible GMRES with the learned right preconditioner P: the Arnoldi step applies
+// M to z_k = P v_k, and the update is x += Z y.
 static GmresResult gmres_lockstep(Solver &S, const double2 *b, double2 *x, double rtol, int restart, int maxiter,
-                                  bool fp32, bool zero_x0, const std::vector<char> &skip, int stall_cycles = 0) {
+                                  bool fp32, bool zero_x0, const std::vector<char> &skip, int stall_cycles = 0,
+                                  bool precond = false) {
   sg_context *c = S.c;
   const int R = S.R;
   const size_t len = S.len();
   restart = std::max(1, std::min(restart, (int)std::min<size_t>(S.rows, kMaxVec - 2)));
   c->w_basis.reserve((size_t)(restart + 1) * len);
+  if (precond) c->w_z.reserve((size_t)restart * len);
+  auto Zk = [&](int k) { return c->w_z.ptr + (size_t)k * len; };
   c->w_w.reserve(len);
   c->w_r.reserve(len);
   c->w_hcol.reserve((size_t)kHcol * R);
@@ -325,8 +330,13 @@ static GmresResult gmres_lockstep(Solver &S, const double2 *b, double2 *x, doubl
       bool all_done = true;
       for (int q = 0; q < R; ++q) all_done &= inner_done[q] != 0;
       if (all_done) break;
-      // w = M v_col
-      S.master(Vk(col), w, fp32);
+      // w = M v_col (flexible: w = M z_col, z_col = P v_col)
+      if (precond) {
+        precond_apply(c, Vk(col), Zk(col), R, S.st);
+        S.master(Zk(col), w, fp32);
+      } else {
+        S.master(Vk(col), w, fp32);
+      }
       res.matvecs++;
       // pass 1: dots with V_0..V_col and w itself (h0^2)
       VecList L{};
@@ -416,7 +426,7 @@ static GmresResult gmres_lockstep(Solver &S, const double2 *b, double2 *x, doubl
       SG_CUDA(cudaMemcpyAsync(dh, ycoef.data(), (size_t)(maxcol + 1) * R * sizeof(double2), cudaMemcpyHostToDevice,
                               S.st));
       VecList L{};
-      for (int k = 0; k <= maxcol; ++k) L.v[k] = Vk(k);
+      for (int k = 0; k <= maxcol; ++k) L.v[k] = precond ? Zk(k) : Vk(k);
       S.combine(L, maxcol + 1, dh, 1.0, x);
     }
     // explicit residual r = b - M x
@@ -851,8 +861,11 @@ static GmresResult block_gmres(Solver &S, const double2 *b, double2 *x, double r
 }
 
 // Mixed precision: FP32-operator GMRES corrections inside FP64 iterative refinement.
+// precond = true makes the correction solves flexible GMRES with the learned preconditioner; a
+// correction that leaves some right-hand side's residual no smaller than it started is redone without
+// it (counted in `fallbacks`), so a poor preconditioner costs time but never the answer.
 static GmresResult refine_mixed(Solver &S, const double2 *b, double2 *x, double rtol, int restart, int maxiter,
-                                int &fp64_mv, int &fp32_mv, int &steps, bool block) {
+                                int &fp64_mv, int &fp32_mv, int &steps, bool block, bool precond, int &fallbacks) {
   sg_context *c = S.c;
   const int R = S.R;
   const size_t len = S.len();
@@ -932,7 +945,22 @@ static GmresResult refine_mixed(Solver &S, const double2 *b, double2 *x, double 
         use_block = false;
       }
     }
-    if (!use_block) g = gmres_lockstep(S, rr, d, tau, restart, cycles, true, true, done, 2);
+    if (!use_block) {
+      g = gmres_lockstep(S, rr, d, tau, restart, cycles, true, true, done, 2, precond);
+      if (precond) {
+        bool failed = false;
+        for (int q = 0; q < R; ++q) failed |= !done[q] && !(g.relres[q] < 1.0);
+        if (failed) {
+          fallbacks++;
+          fp32_mv += g.matvecs;
+          inner_total += g.inner_iters;
+          out.inner_iters += g.inner_iters;
+          out.cycles += g.cycles;
+          k_zero(d, len, S.st);
+          g = gmres_lockstep(S, rr, d, tau, restart, cycles, true, true, done, 2, false);
+        }
+      }
+    }
     fp32_mv += g.matvecs;
     inner_total += g.inner_iters;
     out.inner_iters += g.inner_iters;
@@ -959,10 +987,10 @@ void solve_padded(sg_context *c, const double2 *b, double2 *x, int R, double rto
   SG_CUDA(cudaEventCreate(&ev1));
   SG_CUDA(cudaEventRecord(ev0, st));
   GmresResult g;
-  int fp64_mv = 0, fp32_mv = 0, steps = 0;
+  int fp64_mv = 0, fp32_mv = 0, steps = 0, fallbacks = 0;
   if (precision & SG_FP32) {
     g = refine_mixed(S, b, x, rtol, restart, maxiter * restart, fp64_mv, fp32_mv, steps,
-                     (precision & SG_BLOCK_GMRES) != 0);
+                     (precision & SG_BLOCK_GMRES) != 0, (precision & SG_PRECOND) != 0, fallbacks);
   } else {
     g = gmres_lockstep(S, b, x, rtol, restart, maxiter, false, false, std::vector<char>());
     fp64_mv = g.matvecs;
@@ -987,7 +1015,7 @@ void solve_padded(sg_context *c, const double2 *b, double2 *x, int R, double rto
       mx = std::max(mx, g.relres[q]);
     }
     info->converged = nc;
-    info->reserved = 0;
+    info->precond_fallbacks = fallbacks;
     info->max_rel_residual = mx;
     info->seconds = std::chrono::duration<double>(t1 - t0).count();
     info->device_seconds = dev_ms * 1e-3;

@@ -1,9 +1,11 @@
 // Internal declarations of the smuthi_gb300 CUDA library.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -107,6 +109,17 @@ void k_zero(double2 *p, size_t n, cudaStream_t st);
 // FMA-throughput probe (TFLOP/s) of the FP64 or FP32 pipe
 double fma_peak(int fp64, cudaStream_t st);
 
+// ---------------------------------------------------------------- learned preconditioner (sg_precond.cu)
+int precond_param_count(int bs);
+void precond_add_graph(sg_context *c, int k, const int *nbr_host, int *graph_id, cudaStream_t st);
+void precond_set_params(sg_context *c, int bs, const float *params, int count, cudaStream_t st);
+void precond_get_params(sg_context *c, float *params, int count, cudaStream_t st);
+// z = P v for S padded vectors with the selected graph
+void precond_apply(sg_context *c, const double2 *v, double2 *z, int S, cudaStream_t st);
+void precond_train(sg_context *c, int gid, const double2 *v, const double2 *e, int S, float lr, int step,
+                   double *loss_out, float *grad_host, cudaStream_t st);
+void precond_export_blocks(sg_context *c, int gid, float *G_host, cudaStream_t st);
+
 }  // namespace sg
 
 // ---------------------------------------------------------------- context
@@ -157,6 +170,21 @@ struct sg_context {
   sg::DevBuf<double> w_red;
   sg::DevBuf<double2> w_hcol;
   std::vector<double> h_red;
+
+  // learned preconditioner: k-nearest-neighbour graphs with their near-field blocks T_i W_ij
+  struct PGraph {
+    int n = 0, bs = 0, k1 = 0;  // k1 = neighbours + self
+    sg::DevBuf<int> nbr;        // [n][k1], slot 0 = self
+    sg::DevBuf<int> rev_off, rev_idx;  // edges grouped by their source particle (adjoint)
+    sg::DevBuf<float2> G;       // [n][k1][bs][bs], n2 fastest
+  };
+  std::vector<std::unique_ptr<PGraph>> pgraphs;
+  int p_active = -1, p_bs = 0, p_count = 0;
+  sg::DevBuf<float> p_w, p_g, p_m, p_v;  // FP32 master weights, gradient, Adam moments
+  sg::DevBuf<__nv_bfloat16> p_wb;        // BF16 copy used by the forward and backward kernels
+  sg::DevBuf<float> p_act, p_back;       // activations, backward scratch
+  sg::DevBuf<float2> p_tmp;
+  sg::DevBuf<double2> w_z;               // flexible-GMRES basis Z = P V
 
   // instrumentation
   int64_t launches = 0;

@@ -1,0 +1,269 @@
+"""Learned right preconditioner for the mixed-precision solve.
+
+The reference solves (1 - T W) b = T a with unpreconditioned GMRES
+(smuthi/linearsystem/linear_system.py:285); this module adds an optional learned
+preconditioner P ~ (1 - T W)^{-1} for the flexible GMRES corrections of the mixed
+form (solver flag ``SG_PRECOND``). The network itself, its forward and backward
+passes and the Adam update run in the CUDA library (``sg_precond_*``); this
+module builds the particle graph, the training data and the training loop, and
+stores the weights.
+
+Network (per particle i, per vector): three message-passing layers on the
+k-nearest-neighbour graph, each ``a = sum_s T_i W_{i,nbr(i,s)} h`` (the physical
+near-field coupling, interpolated from the lookup table) followed by an MLP
+``[Re a, Im a, Re h, Im h] -> 128 (ReLU) -> [Re g, Im g]`` and
+``h <- u + alpha a + g``, u the input scaled to unit norm. Weights are stored in
+float32 and used in BF16 by the kernels. With the output weights at zero and
+alpha = 1 it is the Neumann series of the near field, which is the initial state
+before training.
+
+Training pairs (v, e) satisfy v = M e: white random e with v from the FP32
+operator (the default; the loss is then the Frobenius norm of P M - I), or
+exact FP64 Krylov pairs (M^j x, M^{j+1} x) of plane-wave solutions x mixed by
+random coefficients (linearity keeps v = M e).
+"""
+import math
+import os
+
+import numpy as np
+import scipy.spatial
+
+from . import _lib
+
+HIDDEN = 128
+LAYERS = 3
+K_NEIGHBOURS = 16
+DATA_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+
+
+def param_count(blocksize):
+    f, o = 4 * blocksize, 2 * blocksize
+    return LAYERS * (HIDDEN * f + HIDDEN + o * HIDDEN + o + 2)
+
+
+def layer_views(params, blocksize):
+    """Per layer a dict of views into the flat parameter vector: W1 (128 x 4B), b1, W2 (2B x 128), b2, alpha."""
+    f, o = 4 * blocksize, 2 * blocksize
+    out, off = [], 0
+    for _ in range(LAYERS):
+        d = {}
+        d["W1"] = params[off:off + HIDDEN * f].reshape(HIDDEN, f)
+        off += HIDDEN * f
+        d["b1"] = params[off:off + HIDDEN]
+        off += HIDDEN
+        d["W2"] = params[off:off + o * HIDDEN].reshape(o, HIDDEN)
+        off += o * HIDDEN
+        d["b2"] = params[off:off + o]
+        off += o
+        d["alpha"] = params[off:off + 2]
+        off += 2
+        out.append(d)
+    assert off == params.shape[0]
+    return out
+
+
+def init_params(blocksize, seed=0):
+    """Neumann-series start: W2 = b2 = 0, alpha = 1; W1 ~ N(0, 1/(4B))."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    p = np.zeros(param_count(blocksize), np.float32)
+    for d in layer_views(p, blocksize):
+        d["W1"][:] = rng.standard_normal(d["W1"].shape) / math.sqrt(d["W1"].shape[1])
+        d["alpha"][:] = (1.0, 0.0)
+    return p
+
+
+def knn_graph(xy, k=K_NEIGHBOURS):
+    """nbr[i] = [i, k nearest other particles] (int32, n x (k+1)), by lateral distance."""
+    xy = np.ascontiguousarray(np.asarray(xy, dtype=np.float64)[:, :2])
+    n = len(xy)
+    k = max(0, min(k, n - 1))
+    if k == 0:
+        return np.arange(n, dtype=np.int32)[:, None]
+    _, idx = scipy.spatial.cKDTree(xy).query(xy, k=k + 1)
+    idx = np.asarray(idx, dtype=np.int64).reshape(n, k + 1)
+    own = np.arange(n)
+    out = np.empty((n, k + 1), np.int32)
+    out[:, 0] = own
+    for i in range(n):
+        row = idx[i][idx[i] != i][:k]
+        out[i, 1:] = row
+    return out
+
+
+def save_params(params, name, meta=None):
+    os.makedirs(DATA_DIR, exist_ok=True)
+    path = os.path.join(DATA_DIR, name + ".npz")
+    np.savez_compressed(path, params=np.asarray(params, np.float32), **(meta or {}))
+    return path
+
+
+def load_params(name, blocksize):
+    path = os.path.join(DATA_DIR, name + ".npz")
+    d = np.load(path)
+    p = np.ascontiguousarray(d["params"], dtype=np.float32)
+    if p.size != param_count(blocksize):
+        raise ValueError("%s holds %d parameters, blocksize %d needs %d" % (path, p.size, blocksize,
+                                                                             param_count(blocksize)))
+    return p
+
+
+def attach(ctx, xy, blocksize, params, k=K_NEIGHBOURS):
+    """Build the graph of the context's particles, load the weights and select it for SG_PRECOND."""
+    gid = ctx.precond_add_graph(knn_graph(xy, k))
+    ctx.precond_set_params(blocksize, params)
+    ctx.precond_select(gid)
+    return gid
+
+
+# ------------------------------------------------------------------------------------------- systems
+def film_system(name, n_spheres=None, nrhs=16, seed=0, ctx=None, device=0):
+    """A seeded sphere ensemble of workload shape ``name`` set up on a library context.
+
+    Returns a dict with the context, blocksize, lateral positions and the plane-wave right-hand sides
+    (n_unknowns x nrhs, complex128, host).
+    """
+    from . import fields as flds, initial_field as init, layers, particles, workloads
+    from .linearsystem import linear_system as lsm
+    spec = workloads.build(workloads.scaled(name, n_spheres) if n_spheres else name, seed=seed)
+    lm = spec["l_max"]
+    parts = [particles.Sphere(position=list(p), refractive_index=spec["n_particle"], radius=spec["radius"],
+                              l_max=lm, m_max=lm) for p in spec["positions"]]
+    ls = layers.LayerSystem(*spec["layers"])
+    wl = spec["wavelength"]
+    kp = flds.reasonable_Sommerfeld_kpar_contour(wl, layer_refractive_indices=ls.refractive_indices)
+    for p in parts:
+        p.t_matrix = p.compute_t_matrix(wl, ls.refractive_indices[ls.layer_number(p.position[2])])
+    ctx = ctx if ctx is not None else _lib.Context(device)
+    W = lsm.CouplingMatrixRadialLookupCUDA(wl, parts, ls, k_parallel=kp, resolution=spec["resolution"],
+                                           interpolator_kind=spec["kind"], context=ctx)
+    lsm.MasterMatrix(lsm.TMatrix(parts), W)
+    waves = (list(spec["plane_waves"]) + workloads.plane_waves(("random", nrhs), seed + 1))[:nrhs]
+    pos = np.array([p.position for p in parts])
+    tdiag = np.diag(parts[0].t_matrix)
+    rhs = np.stack([(init.PlaneWave(wl, po, az, pl).swe_coefficients(pos, ls, lm, lm) * tdiag[None, :]).ravel()
+                    for (po, az, pl) in waves], axis=1)
+    return dict(ctx=ctx, W=W, blocksize=W.blocksize, xy=pos[:, :2].copy(), rhs=np.ascontiguousarray(rhs),
+                spec=spec, n=len(parts))
+
+
+# ------------------------------------------------------------------------------------------- training
+class TrainingPool:
+    """Training pairs (v, e) with v = M e for one particle set, as device tensors.
+
+    ``white`` batches draw a fresh complex Gaussian e per sample and apply the FP32 operator
+    (v = M e to FP32 accuracy); the loss then averages ||P M e - e||^2 / ||e||^2 over white e, the
+    Frobenius norm of P M - I. ``krylov`` batches mix the exact FP64 pairs (M^j x, M^{j+1} x) of
+    the plane-wave solutions x with random coefficients. ``white_fraction`` sets the share of white
+    samples per batch.
+    """
+
+    def __init__(self, system, white_fraction=1.0, krylov_powers=10, solve_rtol=1e-8, seed=0):
+        import torch
+        ctx = system["ctx"]
+        self.ctx = ctx
+        self.dev = torch.device("cuda", ctx.device)
+        self.white_fraction = white_fraction
+        self.nu = system["rhs"].shape[0]
+        g = torch.Generator(device=self.dev)
+        g.manual_seed(seed)
+        self.gen = g
+        self.ke = self.kv = None
+        if white_fraction < 1.0:
+            dev = self.dev
+            rhs = torch.from_numpy(system["rhs"]).to(dev)
+            R = rhs.shape[1]
+            stream = torch.cuda.current_stream(dev).cuda_stream
+            x = torch.zeros_like(rhs)
+            ctx.gmres_dev(rhs.data_ptr(), x.data_ptr(), R, solve_rtol, restart=64, precision=_lib.SG_FP32,
+                          stream=stream)
+            es, vs = [], []
+            e = x
+            for _ in range(krylov_powers):
+                v = torch.empty_like(e)
+                ctx.master_matvec_dev(e.data_ptr(), v.data_ptr(), R, _lib.SG_FP64, stream=stream)
+                s = torch.linalg.vector_norm(v, dim=0, keepdim=True)
+                es.append(e / s)
+                vs.append(v / s)
+                e = v / s
+            self.ke = torch.stack(es, dim=2)  # nu x R x J: Krylov pairs grouped per right-hand side
+            self.kv = torch.stack(vs, dim=2)
+
+    def white(self, S):
+        import torch
+        e = torch.randn(self.nu, S, dtype=torch.complex128, device=self.dev, generator=self.gen)
+        v = torch.empty_like(e)
+        stream = torch.cuda.current_stream(self.dev).cuda_stream
+        self.ctx.master_matvec_dev(e.data_ptr(), v.data_ptr(), S, _lib.SG_FP32, stream=stream)
+        return v, e
+
+    def krylov(self, S):
+        import torch
+        dev, g = self.dev, self.gen
+        R, J = self.ke.shape[1], self.ke.shape[2]
+        q = torch.randint(0, R, (S,), device=dev, generator=g)
+        c = torch.complex(torch.randn(S, J, device=dev, generator=g, dtype=torch.float64),
+                          torch.randn(S, J, device=dev, generator=g, dtype=torch.float64))
+        return (torch.einsum("nsj,sj->ns", self.kv[:, q, :], c), torch.einsum("nsj,sj->ns", self.ke[:, q, :], c))
+
+    def batch(self, S=16):
+        import torch
+        nw = int(round(S * self.white_fraction))
+        parts = []
+        if nw:
+            parts.append(self.white(nw))
+        if S - nw:
+            parts.append(self.krylov(S - nw))
+        v = torch.cat([p[0] for p in parts], dim=1).contiguous()
+        e = torch.cat([p[1] for p in parts], dim=1).contiguous()
+        return v, e
+
+
+def graph_for(system, k=K_NEIGHBOURS):
+    """Graph id of the k-nearest-neighbour graph of a system's particles (built once per k)."""
+    cache = system.setdefault("graphs", {})
+    if k not in cache:
+        cache[k] = system["ctx"].precond_add_graph(knn_graph(system["xy"], k))
+    return cache[k]
+
+
+def use(system, params, k=K_NEIGHBOURS):
+    """Select the k-nearest-neighbour graph and load ``params`` for SG_PRECOND solves of a system."""
+    gid = graph_for(system, k)
+    system["ctx"].precond_set_params(system["blocksize"], params)
+    system["ctx"].precond_select(gid)
+    return gid
+
+
+def train(system, params, steps=500, lr=1e-3, batch=16, k=K_NEIGHBOURS, pool=None, log_every=50, log=None,
+          seed=0):
+    """Adam training of the preconditioner on one particle set, on the GPU; returns (params, losses)."""
+    import torch
+    ctx, bs = system["ctx"], system["blocksize"]
+    gid = graph_for(system, k)
+    ctx.precond_set_params(bs, params)
+    pool = pool or TrainingPool(system, seed=seed)
+    losses = []
+    for it in range(1, steps + 1):
+        v, e = pool.batch(batch)
+        torch.cuda.synchronize(pool.dev)
+        loss = ctx.precond_train_step(gid, v.data_ptr(), e.data_ptr(), v.shape[1], lr=lr, step=it)
+        losses.append(loss)
+        if log and (it == 1 or it % log_every == 0):
+            log("step %d loss %.4f" % (it, float(np.mean(losses[-log_every:]))))
+    out = ctx.precond_get_params(param_count(bs))
+    ctx.precond_select(gid)
+    return out, losses
+
+
+def evaluate_loss(system, params, pool, batches=8, batch=16, k=K_NEIGHBOURS):
+    """Mean relative error ||P v - e||^2 / ||e||^2 on pool batches (no update)."""
+    import torch
+    ctx, bs = system["ctx"], system["blocksize"]
+    gid = graph_for(system, k)
+    ctx.precond_set_params(bs, params)
+    out = []
+    for _ in range(batches):
+        v, e = pool.batch(batch)
+        torch.cuda.synchronize(pool.dev)
+        out.append(ctx.precond_train_step(gid, v.data_ptr(), e.data_ptr(), v.shape[1], lr=0.0, step=0))
+    return float(np.mean(out))

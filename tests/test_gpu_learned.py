@@ -1,0 +1,220 @@
+"""The learned preconditioner: forward/backward kernels against FP64 autograd, and the solves it drives.
+
+The network's forward pass, loss and gradient from the CUDA kernels are compared with the same
+network written in torch FP64 (autograd for the gradient), using the near-field blocks the library
+built and the BF16-rounded weights the kernels use. Tolerances: forward 1e-4 relative, loss 1e-4,
+gradient 2e-3 relative in total and 5e-3 per weight block (the kernels compute in FP32).
+"""
+import numpy as np
+import pytest
+
+import golden_cases as gc
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(ctx, name="c5s", kind="linear"):
+    from smuthi_gb300 import layers, particles
+    from smuthi_gb300.linearsystem import linear_system as lsm
+    g = gc.load(name)
+    parts = [particles.Sphere(position=list(p), refractive_index=complex(n), radius=float(r), l_max=int(lm),
+                              m_max=int(mm))
+             for p, n, r, lm, mm in zip(g["positions"], g["n_particle"], g["radii"], g["l_max"], g["m_max"])]
+    ln = [complex(x) if complex(x).imag else float(complex(x).real) for x in g["layer_n"]]
+    ls = layers.LayerSystem([float(x) for x in g["thicknesses"]], ln)
+    wl = float(g["wavelength"])
+    W = lsm.CouplingMatrixRadialLookupCUDA(wl, parts, ls, k_parallel=g["kpar"], resolution=float(g["resolution"]),
+                                           interpolator_kind=kind, context=ctx)
+    for p in parts:
+        p.t_matrix = p.compute_t_matrix(wl, ls.refractive_indices[ls.layer_number(p.position[2])])
+    lsm.MasterMatrix(lsm.TMatrix(parts), W)
+    return g, W
+
+
+def _bf16(a):
+    import torch
+    return torch.from_numpy(np.asarray(a, np.float32)).to(torch.bfloat16).to(torch.float64)
+
+
+def _torch_net(G, nbr, params, bs, v):
+    """FP64 restatement of the network: returns (h3, s) for v of shape (n, bs, S)."""
+    import torch
+    from smuthi_gb300 import learned
+    views = learned.layer_views(params, bs)
+    s = torch.sqrt((v.abs() ** 2).sum(dim=(0, 1)))
+    u = v / s
+    h = u
+    nb = torch.from_numpy(nbr.astype(np.int64))
+    for d in views:
+        a = torch.einsum("nkab,nkbs->nas", G, h[nb])
+        f = torch.cat([a.real, a.imag, h.real, h.imag], dim=1).permute(0, 2, 1)
+        p = f @ d["W1"].T + d["b1"]
+        g = (torch.relu(p) @ d["W2"].T + d["b2"]).permute(0, 2, 1)
+        h = u + torch.complex(d["alpha"][0], d["alpha"][1]) * a + torch.complex(g[:, :bs], g[:, bs:])
+    return h, s
+
+
+def _torch_params(params, bs, requires_grad=False):
+    """Flat float64 tensor with W1/W2 rounded to BF16 like the kernels' copies."""
+    import torch
+    from smuthi_gb300 import learned
+    p = torch.from_numpy(np.asarray(params, np.float64).copy())
+    for d, dn in zip(learned.layer_views(p, bs), learned.layer_views(np.asarray(params, np.float32), bs)):
+        d["W1"][:] = _bf16(dn["W1"])
+        d["W2"][:] = _bf16(dn["W2"])
+    return p.requires_grad_(requires_grad)
+
+
+def _trained_like_params(bs, seed=3):
+    from smuthi_gb300 import learned
+    rng = np.random.default_rng(seed)
+    p = learned.init_params(bs, seed=seed)
+    for d in learned.layer_views(p, bs):
+        d["W2"][:] = rng.standard_normal(d["W2"].shape) * 0.02
+        d["b1"][:] = rng.standard_normal(d["b1"].shape) * 0.1
+        d["b2"][:] = rng.standard_normal(d["b2"].shape) * 0.01
+        d["alpha"][:] = (0.9, 0.1)
+    return p
+
+
+def test_forward_and_gradient_match_fp64_autograd(gpu_context):
+    import torch
+    from smuthi_gb300 import learned
+    ctx = gpu_context
+    g, W = _system(ctx)
+    bs, n = W.blocksize, len(g["positions"])
+    nbr = learned.knn_graph(g["positions"], 8)
+    gid = ctx.precond_add_graph(nbr)
+    ctx.precond_select(gid)
+    params = _trained_like_params(bs)
+    ctx.precond_set_params(bs, params)
+    G = torch.from_numpy(ctx.precond_export_blocks(gid, n, nbr.shape[1], bs).astype(np.complex128))
+    rng = np.random.default_rng(5)
+    S = 5
+    V = rng.standard_normal((n * bs, S)) + 1j * rng.standard_normal((n * bs, S))
+    E = rng.standard_normal((n * bs, S)) + 1j * rng.standard_normal((n * bs, S))
+    dev = torch.device("cuda", 0)
+    v_d = torch.from_numpy(V).to(dev)
+    e_d = torch.from_numpy(E).to(dev)
+    z_d = torch.empty_like(v_d)
+    ctx.precond_apply_dev(v_d.data_ptr(), z_d.data_ptr(), S)
+    torch.cuda.synchronize(dev)
+    grad = np.zeros(learned.param_count(bs), np.float32)
+    loss_gpu = ctx.precond_train_step(gid, v_d.data_ptr(), e_d.data_ptr(), S, lr=0.0, step=0, grad=grad)
+
+    pt = _torch_params(params, bs, requires_grad=True)
+    v = torch.from_numpy(V.reshape(n, bs, S))
+    h, s = _torch_net(G, nbr, pt, bs, v)
+    z_ref = (h * s).reshape(n * bs, S).detach().numpy()
+    assert gc.relerr(z_d.cpu().numpy(), z_ref) < 1e-4
+    et = torch.from_numpy(E.reshape(n, bs, S)) / s
+    en = (et.abs() ** 2).sum(dim=(0, 1))
+    loss = (((h - et).abs() ** 2).sum(dim=(0, 1)) / en).mean()
+    loss.backward()
+    assert abs(loss_gpu - loss.item()) <= 1e-4 * abs(loss.item())
+    gref = pt.grad.numpy()
+    assert gc.relerr(grad, gref) < 2e-3
+    for dg, dr in zip(learned.layer_views(grad, bs), learned.layer_views(gref, bs)):
+        for key in ("W1", "b1", "W2", "b2", "alpha"):
+            assert gc.relerr(dg[key], dr[key]) < 5e-3, key
+
+
+def test_neumann_start_is_the_near_field_series(gpu_context):
+    """With W2 = b2 = 0 and alpha = 1 the network is u + A u + A^2 u + A^3 u (times |v|)."""
+    import torch
+    from smuthi_gb300 import learned
+    ctx = gpu_context
+    g, W = _system(ctx)
+    bs, n = W.blocksize, len(g["positions"])
+    nbr = learned.knn_graph(g["positions"], 6)
+    learned.attach(ctx, g["positions"], bs, learned.init_params(bs), k=6)
+    gid = ctx.precond_add_graph(nbr)
+    G = ctx.precond_export_blocks(gid, n, nbr.shape[1], bs).astype(np.complex128)
+    rng = np.random.default_rng(8)
+    V = rng.standard_normal((n * bs, 2)) + 1j * rng.standard_normal((n * bs, 2))
+    dev = torch.device("cuda", 0)
+    v_d = torch.from_numpy(V).to(dev)
+    z_d = torch.empty_like(v_d)
+    ctx.precond_apply_dev(v_d.data_ptr(), z_d.data_ptr(), 2)
+    torch.cuda.synchronize(dev)
+
+    def A(x):
+        x = x.reshape(n, bs, -1)
+        return np.einsum("nkab,nkbs->nas", G, x[nbr]).reshape(n * bs, -1)
+
+    ref = V + A(V) + A(A(V)) + A(A(A(V)))
+    assert gc.relerr(z_d.cpu().numpy(), ref) < 1e-4
+
+
+def test_near_field_blocks_match_the_coupling_operator(gpu_context):
+    """The graph's blocks T_i W_ij equal the FP64 coupling operator restricted to the neighbour pairs."""
+    from smuthi_gb300 import learned
+    ctx = gpu_context
+    g, W = _system(ctx)
+    bs, n = W.blocksize, len(g["positions"])
+    nbr = learned.knn_graph(g["positions"], 4)
+    gid = ctx.precond_add_graph(nbr)
+    G = ctx.precond_export_blocks(gid, n, nbr.shape[1], bs)
+    tdiag = g["t_diag"].reshape(n, bs)
+    for i, j in [(0, int(nbr[0, 1])), (7, int(nbr[7, 3])), (11, 11)]:
+        x = np.zeros(n * bs, complex)
+        cols = []
+        for b in range(bs):
+            x[:] = 0
+            x[j * bs + b] = 1.0
+            cols.append(W.linear_operator.matvec(x)[i * bs:(i + 1) * bs])
+        Wij = np.stack(cols, axis=1)  # includes only pair (i, j) since x is zero elsewhere
+        s = list(nbr[i]).index(j)
+        assert gc.relerr(G[i, s], tdiag[i][:, None] * Wij) < 1e-6
+
+
+def test_preconditioned_mixed_solve_meets_fp64_tolerance(gpu_context):
+    from smuthi_gb300 import _lib, learned
+    ctx = gpu_context
+    g, W = _system(ctx)
+    bs = W.blocksize
+    learned.attach(ctx, g["positions"], bs, learned.init_params(bs))
+    tags = [k[2:] for k in g if k.startswith("b_")]
+    rhs = np.stack([g["rhs_" + t] for t in tags], axis=1)
+    x, info = ctx.gmres(rhs, np.zeros_like(rhs), 1e-6, restart=32, precision=_lib.SG_FP32 | _lib.SG_PRECOND)
+    assert info.converged == rhs.shape[1]
+    assert ctx.true_residual(rhs, x).max() <= 1e-6
+    for k, t in enumerate(tags):
+        assert gc.relerr(x[:, k], g["b_" + t]) < 1e-5
+
+
+def test_bad_preconditioner_falls_back_and_still_converges(gpu_context):
+    from smuthi_gb300 import _lib, learned
+    ctx = gpu_context
+    g, W = _system(ctx)
+    bs = W.blocksize
+    p = learned.init_params(bs)
+    for d in learned.layer_views(p, bs):
+        d["alpha"][:] = (-3.0, 0.0)  # finite but far from any inverse
+    learned.attach(ctx, g["positions"], bs, p)
+    tags = [k[2:] for k in g if k.startswith("b_")]
+    rhs = np.stack([g["rhs_" + t] for t in tags], axis=1)
+    x, info = ctx.gmres(rhs, np.zeros_like(rhs), 1e-6, restart=32, precision=_lib.SG_FP32 | _lib.SG_PRECOND)
+    assert info.converged == rhs.shape[1]
+    assert ctx.true_residual(rhs, x).max() <= 1e-6
+
+
+def test_precond_argument_checks(gpu_context):
+    from smuthi_gb300 import _lib, learned
+    ctx = gpu_context
+    g, W = _system(ctx)
+    bs, n = W.blocksize, len(g["positions"])
+    rhs = np.ascontiguousarray(g["rhs_" + [k[2:] for k in g if k.startswith("b_")][0]])
+    with pytest.raises(_lib.SmuthiGB300Error):  # no graph selected after a new particle set
+        ctx.gmres(rhs, rhs, 1e-6, precision=_lib.SG_FP32 | _lib.SG_PRECOND)
+    bad = learned.knn_graph(g["positions"], 3)
+    bad[5, 0] = 4  # slot 0 must be the particle itself
+    with pytest.raises(_lib.SmuthiGB300Error):
+        ctx.precond_add_graph(bad)
+    bad = learned.knn_graph(g["positions"], 3)
+    bad[2, 2] = n  # out of range
+    with pytest.raises(_lib.SmuthiGB300Error):
+        ctx.precond_add_graph(bad)
+    with pytest.raises(_lib.SmuthiGB300Error):
+        ctx.precond_set_params(bs, np.zeros(learned.param_count(bs) - 1, np.float32))
+    assert _lib.lib().sg_precond_param_count(bs) == learned.param_count(bs)
