@@ -863,7 +863,8 @@ static GmresResult block_gmres(Solver &S, const double2 *b, double2 *x, double r
 // Mixed precision: FP32-operator GMRES corrections inside FP64 iterative refinement.
 // precond = true makes the correction solves flexible GMRES with the learned preconditioner; a
 // correction that leaves some right-hand side's residual no smaller than it started is redone without
-// it (counted in `fallbacks`), so a poor preconditioner costs time but never the answer.
+// it, and a refinement step that fails to halve the FP64 residual turns the preconditioner off for the
+// rest of the solve (both counted in `fallbacks`), so a poor preconditioner costs time, not the answer.
 static GmresResult refine_mixed(Solver &S, const double2 *b, double2 *x, double rtol, int restart, int maxiter,
                                 int &fp64_mv, int &fp32_mv, int &steps, bool block, bool precond, int &fallbacks) {
   sg_context *c = S.c;
@@ -925,7 +926,13 @@ static GmresResult refine_mixed(Solver &S, const double2 *b, double2 *x, double 
     if (worst == 0.0 || steps == max_steps || inner_total >= maxiter) break;
     // refinement must contract the FP64 residual; two steps without halving it end the solve
     if (steps > 0 && worst > 0.5 * prev_worst) {
-      if (++no_progress >= 2) break;
+      if (precond) {
+        // the preconditioned corrections stopped contracting the FP64 residual: finish without them
+        precond = false;
+        fallbacks++;
+      } else if (++no_progress >= 2) {
+        break;
+      }
     } else {
       no_progress = 0;
     }

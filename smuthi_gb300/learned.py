@@ -90,9 +90,10 @@ def knn_graph(xy, k=K_NEIGHBOURS):
     return out
 
 
-def save_params(params, name, meta=None):
-    os.makedirs(DATA_DIR, exist_ok=True)
-    path = os.path.join(DATA_DIR, name + ".npz")
+def save_params(params, name, meta=None, directory=None):
+    directory = directory or DATA_DIR
+    os.makedirs(directory, exist_ok=True)
+    path = os.path.join(directory, name + ".npz")
     np.savez_compressed(path, params=np.asarray(params, np.float32), **(meta or {}))
     return path
 
@@ -234,25 +235,72 @@ def use(system, params, k=K_NEIGHBOURS):
     return gid
 
 
+def alpha_mask(blocksize):
+    """Mask selecting only the per-layer alpha coefficients (the near-field polynomial)."""
+    m = np.zeros(param_count(blocksize), np.float32)
+    for d in layer_views(m, blocksize):
+        d["alpha"][:] = 1.0
+    return m
+
+
 def train(system, params, steps=500, lr=1e-3, batch=16, k=K_NEIGHBOURS, pool=None, log_every=50, log=None,
-          seed=0):
-    """Adam training of the preconditioner on one particle set, on the GPU; returns (params, losses)."""
+          seed=0, mask=None):
+    """Adam training of the preconditioner on one particle set; returns (params, losses).
+
+    Forward and backward passes always run in the library's kernels. Without ``mask`` the Adam step
+    runs on the device too; with a 0/1 ``mask`` only the masked parameters move, and the (cheap)
+    Adam step is taken on the host from the device gradient.
+    """
     import torch
     ctx, bs = system["ctx"], system["blocksize"]
     gid = graph_for(system, k)
-    ctx.precond_set_params(bs, params)
+    p = np.ascontiguousarray(params, dtype=np.float32).copy()
+    ctx.precond_set_params(bs, p)
     pool = pool or TrainingPool(system, seed=seed)
     losses = []
+    if mask is not None:
+        m1 = np.zeros_like(p)
+        m2 = np.zeros_like(p)
+        grad = np.zeros_like(p)
     for it in range(1, steps + 1):
         v, e = pool.batch(batch)
         torch.cuda.synchronize(pool.dev)
-        loss = ctx.precond_train_step(gid, v.data_ptr(), e.data_ptr(), v.shape[1], lr=lr, step=it)
+        if mask is None:
+            loss = ctx.precond_train_step(gid, v.data_ptr(), e.data_ptr(), v.shape[1], lr=lr, step=it)
+        else:
+            loss = ctx.precond_train_step(gid, v.data_ptr(), e.data_ptr(), v.shape[1], lr=0.0, step=0, grad=grad)
+            gm = grad * mask
+            m1 = 0.9 * m1 + 0.1 * gm
+            m2 = 0.999 * m2 + 0.001 * gm * gm
+            p = (p - lr * (m1 / (1 - 0.9 ** it)) / (np.sqrt(m2 / (1 - 0.999 ** it)) + 1e-8)).astype(np.float32)
+            ctx.precond_set_params(bs, p)
         losses.append(loss)
         if log and (it == 1 or it % log_every == 0):
             log("step %d loss %.4f" % (it, float(np.mean(losses[-log_every:]))))
     out = ctx.precond_get_params(param_count(bs))
     ctx.precond_select(gid)
     return out, losses
+
+
+def solve_iterations(system, params=None, nrhs=16, rtol=1e-6, restart=64, k=K_NEIGHBOURS):
+    """Mixed-form solve of the system's plane-wave right-hand sides, with the preconditioner when
+    ``params`` is given; returns the solver report and the FP64-true residuals."""
+    import torch
+    ctx = system["ctx"]
+    prec = _lib.SG_FP32
+    if params is not None:
+        use(system, params, k)
+        prec |= _lib.SG_PRECOND
+    dev = torch.device("cuda", ctx.device)
+    rhs = np.ascontiguousarray(system["rhs"][:, :nrhs])
+    b = torch.from_numpy(rhs).to(dev)
+    x = torch.zeros_like(b)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    info = ctx.gmres_dev(b.data_ptr(), x.data_ptr(), b.shape[1], rtol, restart=restart, precision=prec,
+                         stream=stream)
+    torch.cuda.synchronize(dev)
+    rel = ctx.true_residual(rhs, np.ascontiguousarray(x.cpu().numpy()))
+    return info.as_dict(), rel
 
 
 def evaluate_loss(system, params, pool, batches=8, batch=16, k=K_NEIGHBOURS):
@@ -267,3 +315,60 @@ def evaluate_loss(system, params, pool, batches=8, batch=16, k=K_NEIGHBOURS):
         torch.cuda.synchronize(pool.dev)
         out.append(ctx.precond_train_step(gid, v.data_ptr(), e.data_ptr(), v.shape[1], lr=0.0, step=0))
     return float(np.mean(out))
+
+
+# ------------------------------------------------------------------------------------------- weights
+def fit_film_weights(name="c5", n_train=1000, n_val=2000, seed_train=11, seed_val=12, k=K_NEIGHBOURS, log=print):
+    """Train candidate weights for a workload shape and keep the one with the fewest held-out iterations.
+
+    Candidates: the Neumann start; the per-layer alphas trained on the Frobenius objective; full
+    networks fine-tuned from those alphas at two learning rates. Selection is by the FGMRES iteration
+    count of the mixed solve of 16 plane waves on a held-out particle set (``n_val`` spheres,
+    another seed), because a lower training loss does not by itself mean fewer iterations.
+    Returns (best params, report dict).
+    """
+    tr = film_system(name, n_train, nrhs=16, seed=seed_train)
+    val = film_system(name, n_val, nrhs=16, seed=seed_val)
+    bs = tr["blocksize"]
+    base, _ = solve_iterations(val)
+    report = {"shape": name, "n_train": n_train, "n_val": n_val, "k": k, "val_unpreconditioned": base}
+    log("unpreconditioned: %d iterations" % base["iterations"])
+    cands = {"neumann": init_params(bs)}
+    pool = TrainingPool(tr, white_fraction=1.0, seed=1)
+    cands["alpha"], _ = train(tr, cands["neumann"], steps=300, lr=1e-2, k=k, pool=pool, mask=alpha_mask(bs))
+    for lr in (1e-5, 3e-5):
+        cands["full_%g" % lr], _ = train(tr, cands["alpha"], steps=400, lr=lr, k=k, pool=pool)
+    best, best_it = None, None
+    for tag, p in cands.items():
+        info, rel = solve_iterations(val, p, k=k)
+        report["val_" + tag] = info
+        ok = info["converged"] == 16 and float(rel.max()) <= 1e-6
+        log("%s: %d iterations, %d fallbacks, %.3f s, ok %s" % (tag, info["iterations"], info["precond_fallbacks"],
+                                                               info["device_seconds"], ok))
+        if ok and info["precond_fallbacks"] == 0 and (best_it is None or info["iterations"] < best_it):
+            best, best_it = tag, info["iterations"]
+    if best is None:  # nothing beat the fallback-free bar: keep the physics start
+        best = "neumann"
+    report["selected"] = best
+    return cands[best], report
+
+
+def main(argv=None):
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="train the learned preconditioner for a workload shape")
+    ap.add_argument("--shape", default="c5")
+    ap.add_argument("--n-train", type=int, default=1000)
+    ap.add_argument("--n-val", type=int, default=2000)
+    ap.add_argument("--out", default=None, help="weights name (default film_<shape>)")
+    ap.add_argument("--dir", default=None, help="output directory (default: the package data directory)")
+    a = ap.parse_args(argv)
+    p, rep = fit_film_weights(a.shape, a.n_train, a.n_val)
+    name = a.out or "film_%s" % a.shape
+    path = save_params(p, name, meta={"report": json.dumps(rep, default=float)}, directory=a.dir)
+    print(json.dumps(rep, default=float))
+    print("wrote", path)
+
+
+if __name__ == "__main__":
+    main()

@@ -218,3 +218,16 @@ def test_precond_argument_checks(gpu_context):
     with pytest.raises(_lib.SmuthiGB300Error):
         ctx.precond_set_params(bs, np.zeros(learned.param_count(bs) - 1, np.float32))
     assert _lib.lib().sg_precond_param_count(bs) == learned.param_count(bs)
+
+
+def test_committed_weights_reduce_iterations_on_held_out_film(gpu_context):
+    """The shipped weights (selected on another particle set) cut the mixed solve's iterations on a
+    film ensemble none of the training or selection runs saw, at the same FP64-true tolerance."""
+    from smuthi_gb300 import learned
+    val = learned.film_system("c5", 1000, nrhs=16, seed=31, ctx=gpu_context)
+    weights = learned.load_params("film_c5", val["blocksize"])
+    base, rel0 = learned.solve_iterations(val)
+    info, rel = learned.solve_iterations(val, weights)
+    assert rel0.max() <= 1e-6 and rel.max() <= 1e-6
+    assert info["converged"] == 16 and info["precond_fallbacks"] == 0
+    assert info["iterations"] < base["iterations"]
