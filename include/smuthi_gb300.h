@@ -45,6 +45,12 @@ extern "C" {
  * right-preconditioned flexible GMRES with the learned preconditioner selected by
  * sg_precond_select; a correction solve that fails to reduce its residual is redone without it */
 #define SG_PRECOND 4
+/* double-float arithmetic: every sum of the coupling operator in two FP32 words (about 48
+ * significant bits) on the FP32 pipe, with the FP64 table split into two FP32 words. As a matvec
+ * precision it is an FP64-grade operator (it agrees with SG_FP64 to ~1e-13 relative); OR-ed into
+ * sg_gmres_solve's precision with SG_FP32, the refinement's true residuals use it in place of the
+ * FP64 operator. No counterpart in the reference. */
+#define SG_DF64 8
 
 typedef struct sg_context sg_context;
 
@@ -130,7 +136,7 @@ int sg_true_residual(sg_context *ctx, const double *b, const double *x, int nrhs
 /* Kernel instrumentation. sg_profile(ctx, 1) brackets every coupling-kernel
  * launch with CUDA events on its stream; sg_kernel_timing synchronises and
  * returns the summed event time (ms) and the number of bracketed launches
- * of the given precision (SG_FP64, SG_FP32, or -1 for both) since the last
+ * of the given precision (SG_FP64, SG_FP32, SG_DF64, or -1 for all) since the last
  * reset. sg_launch_count returns the number of kernels this context has
  * launched since it was created. */
 int sg_profile(sg_context *ctx, int enable);

@@ -204,6 +204,7 @@ int sg_set_lookup(sg_context *ctx, int kind, int len_rho, double rho_min, double
     ctx->rho_min = rho_min;
     ctx->res = resolution;
     ctx->pairs_ready = false;
+    ctx->df_ready = false;
     ctx->pgraphs.clear();  // their near-field blocks came from the old table
     ctx->p_active = -1;
     return SG_OK;
@@ -264,7 +265,7 @@ static void matvec_dev(sg_context *c, const double2 *x, double2 *y, int R, int p
                        cudaStream_t st) {
   require_ready(c, master);
   SG_REQUIRE(R >= 1 && R <= 256, "nrhs must be in [1, 256]");
-  SG_REQUIRE(precision == SG_FP64 || precision == SG_FP32, "unknown precision");
+  SG_REQUIRE(precision == SG_FP64 || precision == SG_FP32 || precision == SG_DF64, "unknown precision");
   use_device(c);
   const bool fp32 = precision == SG_FP32;
   if (fp32) ensure_pairs(c, st);
@@ -274,7 +275,8 @@ static void matvec_dev(sg_context *c, const double2 *x, double2 *y, int R, int p
     c->pad_out.reserve(c->padded(R));
     yp = c->pad_out.ptr;
   }
-  sg::apply_padded(c, xp, yp, R, master, fp32, st);
+  if (precision == SG_DF64) sg::apply_padded_df64(c, xp, yp, R, master, st);
+  else sg::apply_padded(c, xp, yp, R, master, fp32, st);
   if (!c->uniform) {
     sg::k_scatter(yp, y, c->map.ptr, c->n_unknowns, R, st);
     c->launches += 1;
@@ -332,8 +334,9 @@ static int solve_dev_impl(sg_context *ctx, const double2 *b, double2 *x, int nrh
   SG_REQUIRE(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
   SG_REQUIRE(rtol > 0 && std::isfinite(rtol), "rtol must be positive");
   SG_REQUIRE(restart >= 0 && restart <= 128, "restart must be in [0, 128] (0 = 20)");
-  SG_REQUIRE(precision == SG_FP64 || precision == SG_FP32 || precision == (SG_FP32 | SG_BLOCK_GMRES) ||
-                 precision == (SG_FP32 | SG_PRECOND),
+  SG_REQUIRE(precision == SG_FP64 ||
+                 ((precision & SG_FP32) && !(precision & ~(SG_FP32 | SG_BLOCK_GMRES | SG_PRECOND | SG_DF64)) &&
+                  !((precision & SG_BLOCK_GMRES) && (precision & SG_PRECOND))),
              "unknown precision / solver flags");
   if (precision & SG_PRECOND) {
     SG_REQUIRE(ctx->p_active >= 0, "SG_PRECOND needs a preconditioner graph (sg_precond_select)");
@@ -432,7 +435,8 @@ int sg_profile(sg_context *ctx, int enable) {
 int sg_kernel_timing(sg_context *ctx, int precision, double *total_ms, int64_t *count, int reset) {
   return guarded([&]() -> int {
     SG_REQUIRE(ctx != nullptr, "null context");
-    SG_REQUIRE(precision >= -1 && precision <= 1, "precision must be SG_FP64, SG_FP32 or -1 (both)");
+    SG_REQUIRE(precision == -1 || precision == SG_FP64 || precision == SG_FP32 || precision == SG_DF64,
+               "precision must be SG_FP64, SG_FP32, SG_DF64 or -1 (all)");
     use_device(ctx);
     for (auto &ev : ctx->events) {
       SG_CUDA(cudaEventSynchronize(ev.e1));
@@ -444,7 +448,8 @@ int sg_kernel_timing(sg_context *ctx, int precision, double *total_ms, int64_t *
       cudaEventDestroy(ev.e1);
     }
     ctx->events.clear();
-    const int lo = precision < 0 ? 0 : precision, hi = precision < 0 ? 1 : precision;
+    const int slot = precision == SG_DF64 ? 2 : precision;
+    const int lo = precision < 0 ? 0 : slot, hi = precision < 0 ? 2 : slot;
     double ms = 0.0;
     int64_t n = 0;
     for (int p = lo; p <= hi; ++p) {
@@ -454,8 +459,8 @@ int sg_kernel_timing(sg_context *ctx, int precision, double *total_ms, int64_t *
     if (total_ms) *total_ms = ms;
     if (count) *count = n;
     if (reset) {
-      ctx->coupling_ms[0] = ctx->coupling_ms[1] = 0.0;
-      ctx->coupling_launches[0] = ctx->coupling_launches[1] = 0;
+      ctx->coupling_ms[0] = ctx->coupling_ms[1] = ctx->coupling_ms[2] = 0.0;
+      ctx->coupling_launches[0] = ctx->coupling_launches[1] = ctx->coupling_launches[2] = 0;
     }
     return SG_OK;
   });

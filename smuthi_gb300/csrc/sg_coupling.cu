@@ -15,12 +15,17 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "sg_df64.h"
 #include "sg_internal.h"
 
 namespace sg {
 
 template <typename Real>
 struct CT;
+template <>
+struct CT<df64> {
+  typedef df64x2 T;  // 16 bytes: (re.hi, re.lo, im.hi, im.lo)
+};
 template <>
 struct CT<double> {
   typedef double2 T;
@@ -31,6 +36,17 @@ struct CT<float> {
 };
 
 static constexpr int kThreads = 256;
+
+// read-only cached coefficient loads
+__device__ __forceinline__ double2 ldc(const double2 *p) { return __ldg(p); }
+__device__ __forceinline__ float2 ldc(const float2 *p) { return __ldg(p); }
+__device__ __forceinline__ df64x2 ldc(const df64x2 *p) {
+  const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+  df64x2 r;
+  r.x = df64(v.x, v.y);
+  r.y = df64(v.z, v.w);
+  return r;
+}
 
 int coef_count(int kind) { return kind == SG_LINEAR ? 2 : 4; }
 
@@ -170,11 +186,11 @@ __global__ void __launch_bounds__(kThreads) coupling_kernel(const CouplingLaunch
 #pragma unroll
       for (int q = 0; q < P; ++q) {
         const cplx *cp = cbase + (size_t)n2 * bs + nrowc[q];
-        cplx cc = __ldg(cp + (NC - 1) * bs2);
+        cplx cc = ldc(cp + (NC - 1) * bs2);
         Real lr = cc.x, li = cc.y;
 #pragma unroll
         for (int ci = NC - 2; ci >= 0; --ci) {
-          const cplx d = __ldg(cp + ci * bs2);
+          const cplx d = ldc(cp + ci * bs2);
           lr = fma(lr, t, d.x);
           li = fma(li, t, d.y);
         }
@@ -312,6 +328,35 @@ int choose_split(int n_particles, int nrhs) {
   if (s > maxs) s = maxs;
   (void)nrhs;
   return s;
+}
+
+// FP64-grade coupling sums in double-float arithmetic on the FP32 pipe; L.coef holds the FP64
+// coefficients split into two FP32 words (df64x2), positions and vectors stay FP64.
+int launch_coupling_df64(const CouplingLaunch &L, int nsplit, cudaStream_t st) {
+  SG_REQUIRE(L.bs >= 1 && L.bs <= 96, "blocksize must be in [1, 96]");
+  SG_REQUIRE(L.ncoef == 2 || L.ncoef == 4, "bad coefficient count");
+  const int R = L.nrhs;
+  if (L.ncoef == 2) {
+    if (R % 4 == 0) launch_p<df64, 2, 4, false>(L, nsplit, st);
+    else if (R % 2 == 0) launch_p<df64, 2, 2, false>(L, nsplit, st);
+    else launch_p<df64, 2, 1, false>(L, nsplit, st);
+  } else {
+    if (R % 4 == 0) launch_p<df64, 4, 4, false>(L, nsplit, st);
+    else if (R % 2 == 0) launch_p<df64, 4, 2, false>(L, nsplit, st);
+    else launch_p<df64, 4, 1, false>(L, nsplit, st);
+  }
+  return nsplit > 1 ? 2 : 1;
+}
+
+// df64x2 copy of the FP64 coefficients
+__global__ void coef_to_df64_kernel(const double2 *src, df64x2 *dst, size_t n) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) dst[e] = df_from_double2(src[e]);
+}
+
+void build_coefficients_df64(const double2 *coef64, void *coefdf, size_t n, cudaStream_t st) {
+  coef_to_df64_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(coef64, reinterpret_cast<df64x2 *>(coefdf), n);
+  SG_CUDA(cudaGetLastError());
 }
 
 int launch_coupling(const CouplingLaunch &L, bool fp32, int nsplit, cudaStream_t st) {

@@ -1,0 +1,96 @@
+// Double-float ("df64") arithmetic on the FP32 pipe.
+//
+// A df64 value is the unevaluated sum hi + lo of two FP32 numbers with |lo| <= ulp(hi) / 2, which
+// carries about 48 significant bits. The operations are built from the classical error-free
+// transformations: TwoSum (Knuth, TAOCP vol. 2, 4.2.2), Fast2Sum (Dekker, 1971) and the exact
+// product through a fused multiply-add (a * b = p + fma(a, b, -p)). Products drop the lo * lo term
+// and sums use the "sloppy" double-word addition (one TwoSum on the high words), as analysed by
+// Joldes, Muller and Popescu, "Tight and rigorous error bounds for basic building blocks of
+// double-word arithmetic", ACM TOMS 44(2), 2017: the absolute error of a sum is a small multiple of
+// 2^-46 (|a| + |b|), which is what an accumulation of many terms needs.
+//
+// On GB300 the FP32 pipe issues 59x the FP64 pipe's FMAs; a df64 FMA costs about 15 FP32
+// instructions, so FP64-grade coupling sums run several times faster in df64 than in FP64.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace sg {
+// The type and its operations live in a nested namespace: argument-dependent lookup finds this fma()
+// for df64 arguments only, and an unqualified fma() on double or float arguments inside namespace sg
+// still resolves to the CUDA math overloads.
+namespace dfw {
+
+struct df64 {
+  float hi, lo;
+  __host__ __device__ df64() {}
+  __host__ __device__ df64(float h, float l) : hi(h), lo(l) {}
+  __device__ df64(int v) : hi((float)v), lo(0.f) {}
+  __device__ df64(float v) : hi(v), lo(0.f) {}
+  __device__ df64(double d) {
+    hi = (float)d;
+    lo = (float)(d - (double)hi);
+  }
+  __device__ explicit operator double() const { return (double)hi + (double)lo; }
+  __device__ explicit operator float() const { return hi + lo; }
+};
+
+struct df64x2 {
+  df64 x, y;
+};
+
+// s + e == a + b exactly
+__device__ __forceinline__ df64 df_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  const float e = (a - (s - bb)) + (b - bb);
+  return df64(s, e);
+}
+
+// s + e == a + b exactly when |a| >= |b|
+__device__ __forceinline__ df64 df_fast_two_sum(float a, float b) {
+  const float s = a + b;
+  const float e = b - (s - a);
+  return df64(s, e);
+}
+
+__device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
+
+__device__ __forceinline__ df64 operator+(df64 a, df64 b) {
+  const df64 s = df_two_sum(a.hi, b.hi);
+  return df_fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+}
+
+__device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }
+
+__device__ __forceinline__ df64 operator*(df64 a, df64 b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return df_fast_two_sum(p, e);
+}
+
+// a * b + c
+__device__ __forceinline__ df64 fma(df64 a, df64 b, df64 c) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const df64 s = df_two_sum(c.hi, p);
+  return df_fast_two_sum(s.hi, s.lo + (c.lo + e));
+}
+
+// FP64 complex -> df64 complex (hi = nearest float, lo = nearest float of the remainder)
+__device__ __forceinline__ df64x2 df_from_double2(double2 v) {
+  df64x2 r;
+  r.x = df64(v.x);
+  r.y = df64(v.y);
+  return r;
+}
+
+}  // namespace dfw
+using dfw::df64;
+using dfw::df64x2;
+using dfw::df_from_double2;
+}  // namespace sg

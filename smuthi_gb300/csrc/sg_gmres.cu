@@ -157,6 +157,11 @@ struct Solver {
 
   // y = M x on padded vectors with the FP64 or FP32 operator
   void master(const double2 *x, double2 *y, bool fp32) { apply_padded(c, x, y, R, true, fp32, st); }
+  // y = M x with FP64-grade sums: the FP64 operator, or its double-float twin when df64 is set
+  void master_true(const double2 *x, double2 *y, bool df64) {
+    if (df64) apply_padded_df64(c, x, y, R, true, st);
+    else apply_padded(c, x, y, R, true, false, st);
+  }
 
   // out[k][r] = <V_k, w> for k < nvec (device), copied to host h (nvec * R)
   void dots(const VecList &V, int nvec, const double2 *w, double2 *dout) {
@@ -866,7 +871,8 @@ static GmresResult block_gmres(Solver &S, const double2 *b, double2 *x, double r
 // it, and a refinement step that fails to halve the FP64 residual turns the preconditioner off for the
 // rest of the solve (both counted in `fallbacks`), so a poor preconditioner costs time, not the answer.
 static GmresResult refine_mixed(Solver &S, const double2 *b, double2 *x, double rtol, int restart, int maxiter,
-                                int &fp64_mv, int &fp32_mv, int &steps, bool block, bool precond, int &fallbacks) {
+                                int &fp64_mv, int &fp32_mv, int &steps, bool block, bool precond, int &fallbacks,
+                                bool df64) {
   sg_context *c = S.c;
   const int R = S.R;
   const size_t len = S.len();
@@ -904,7 +910,7 @@ static GmresResult refine_mixed(Solver &S, const double2 *b, double2 *x, double 
     if (steps == 0 && x0_zero) {
       SG_CUDA(cudaMemcpyAsync(rr, b, len * sizeof(double2), cudaMemcpyDeviceToDevice, S.st));
     } else {
-      S.master(x, rr, false);
+      S.master_true(x, rr, df64);
       fp64_mv++;
       sub_from_kernel<<<nblocks(len), 256, 0, S.st>>>(b, rr, len);
       SG_CUDA(cudaGetLastError());
@@ -997,7 +1003,8 @@ void solve_padded(sg_context *c, const double2 *b, double2 *x, int R, double rto
   int fp64_mv = 0, fp32_mv = 0, steps = 0, fallbacks = 0;
   if (precision & SG_FP32) {
     g = refine_mixed(S, b, x, rtol, restart, maxiter * restart, fp64_mv, fp32_mv, steps,
-                     (precision & SG_BLOCK_GMRES) != 0, (precision & SG_PRECOND) != 0, fallbacks);
+                     (precision & SG_BLOCK_GMRES) != 0, (precision & SG_PRECOND) != 0, fallbacks,
+                     (precision & SG_DF64) != 0);
   } else {
     g = gmres_lockstep(S, b, x, rtol, restart, maxiter, false, false, std::vector<char>());
     fp64_mv = g.matvecs;
@@ -1127,6 +1134,50 @@ void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool maste
   if (c->profiling) {
     SG_CUDA(cudaEventRecord(e1, st));
     c->events.push_back({e0, e1, fp32 ? 1 : 0});
+  }
+}
+
+void apply_padded_df64(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st) {
+  const size_t ncoef_total = (size_t)c->n_int * c->ncoef * c->bs * c->bs;
+  if (!c->df_ready) {
+    c->coefdf.reserve(ncoef_total);
+    build_coefficients_df64(c->coef64.ptr, c->coefdf.ptr, ncoef_total, st);
+    c->launches += 1;
+    c->df_ready = true;
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (c->profiling) {
+    SG_CUDA(cudaEventCreate(&e0));
+    SG_CUDA(cudaEventCreate(&e1));
+    SG_CUDA(cudaEventRecord(e0, st));
+  }
+  CouplingLaunch L{};
+  L.pos = c->pos.ptr;
+  L.mofn = c->mofn.ptr;
+  L.coef = c->coefdf.ptr;
+  L.pairs = nullptr;
+  L.n = c->n;
+  L.bs = c->bs;
+  L.n_int = c->n_int;
+  L.ncoef = c->ncoef;
+  L.rho_min = c->rho_min;
+  L.res = c->res;
+  L.x = x;
+  L.y = y;
+  L.nrhs = R;
+  L.master = master ? 1 : 0;
+  L.t = c->tmat.ptr;
+  L.ptype = c->ptype.ptr;
+  L.t_diag = c->t_diag;
+  const int ns = choose_split(c->n, R);
+  if (ns > 1) {
+    c->w_partial.reserve((size_t)ns * c->n * c->bs * R);
+    L.partial = c->w_partial.ptr;
+  }
+  c->launches += launch_coupling_df64(L, ns, st);
+  if (c->profiling) {
+    SG_CUDA(cudaEventRecord(e1, st));
+    c->events.push_back({e0, e1, 2});
   }
 }
 

@@ -81,6 +81,11 @@ struct CouplingLaunch {
 
 // launch the coupling matvec on padded vectors; returns number of kernels launched
 int launch_coupling(const CouplingLaunch &L, bool fp32, int nsplit, cudaStream_t st);
+// the same in double-float arithmetic (L.coef = df64 coefficients from build_coefficients_df64)
+int launch_coupling_df64(const CouplingLaunch &L, int nsplit, cudaStream_t st);
+void build_coefficients_df64(const double2 *coef64, void *coefdf, size_t n, cudaStream_t st);
+// y = M x or W x in double-float arithmetic (FP64-grade; builds the df64 coefficients on first use)
+void apply_padded_df64(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st);
 // padded-vector operator application and solver (sg_gmres.cu)
 void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool master, bool fp32, cudaStream_t st);
 void solve_padded(sg_context *c, const double2 *b, double2 *x, int R, double rtol, int restart, int maxiter,
@@ -142,6 +147,8 @@ struct sg_context {
   sg::DevBuf<double2> coef64;
   sg::DevBuf<float2> coef32;
   sg::DevBuf<int4> pairs;
+  sg::DevBuf<double2> coefdf;  // FP64 coefficients split into two FP32 words each (16 bytes per complex)
+  bool df_ready = false;
   bool pairs_ready = false;  // FP32 operator data (bucket plan or pair table) is built
 
   // interval-bucketed FP32 operator (sg_bucket.cu)
@@ -194,8 +201,8 @@ struct sg_context {
     int fp32;
   };
   std::vector<Timed> events;
-  int64_t coupling_launches[2] = {0, 0};  // [fp64, fp32]
-  double coupling_ms[2] = {0.0, 0.0};
+  int64_t coupling_launches[3] = {0, 0, 0};  // [fp64, fp32, df64]
+  double coupling_ms[3] = {0.0, 0.0, 0.0};
 
   size_t padded(int nrhs) const { return (size_t)n * bs * nrhs; }
 };

@@ -236,3 +236,35 @@ def test_block_gmres_mixed(name, gpu_context):
         bk = "b_" + k[4:]
         if bk in g:
             assert gc.relerr(X[:, q], g[bk]) < 1e-4
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_df64_operator_matches_fp64(name, gpu_context):
+    """The double-float operator (two FP32 words per value on the FP32 pipe) is FP64-grade."""
+    from smuthi_gb300 import _lib
+    g = gc.load(name)
+    for kind in _kinds(g):
+        parts, ls, wl, W, M = _product_system(g, kind, gpu_context)
+        x = g["x_" + kind]
+        assert gc.relerr(gpu_context.coupling_matvec(x, _lib.SG_DF64), gpu_context.coupling_matvec(x, 0)) < 1e-12
+        assert gc.relerr(gpu_context.coupling_matvec(x, _lib.SG_DF64), g["Wx_" + kind]) < 1e-12
+        assert gc.relerr(gpu_context.master_matvec(x, _lib.SG_DF64), g["Mx_" + kind]) < 1e-12
+        X = np.ascontiguousarray(np.stack([x, 1j * x, x.conj()], axis=1))  # RHS tiles of 1, 2, 4 columns
+        Y = gpu_context.master_matvec(X, _lib.SG_DF64)
+        assert gc.relerr(Y, gpu_context.master_matvec(X, 0)) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["c1", "c5s", "c3s"])
+def test_mixed_solution_with_df64_residuals(name, gpu_context):
+    """Refinement residuals in double-float still give an FP64-true residual below the tolerance."""
+    from smuthi_gb300 import _lib
+    g = gc.load(name)
+    keys = sorted(k for k in g if k.startswith("b_"))
+    kind = keys[0][2:].split("_w")[0]
+    parts, ls, wl, W, M = _product_system(g, kind, gpu_context)
+    B = np.ascontiguousarray(np.stack([g["rhs_" + k[2:]] for k in keys], axis=1))
+    X, info = gpu_context.gmres(B, np.zeros_like(B), 1e-6, restart=20, precision=_lib.SG_FP32 | _lib.SG_DF64)
+    assert info.converged == B.shape[1]
+    assert gpu_context.true_residual(B, X).max() <= 1e-6
+    for q, k in enumerate(keys):
+        assert gc.relerr(X[:, q], g[k]) < 1e-4
