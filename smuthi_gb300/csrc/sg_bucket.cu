@@ -162,6 +162,11 @@ __global__ void to_f32_kernel(const double2 *x, float2 *y, size_t n) {
   if (e < n) y[e] = make_float2((float)x[e].x, (float)x[e].y);
 }
 
+void k_to_f32(const double2 *x, float2 *y, size_t n, cudaStream_t st) {
+  to_f32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(x, y, n);
+  SG_CUDA(cudaGetLastError());
+}
+
 struct BucketArgs {
   const int *members;
   const int4 *rec;

@@ -157,11 +157,25 @@ __global__ void __launch_bounds__(kThreads) coupling_kernel(const CouplingLaunch
 #pragma unroll
     for (int q = 0; q < P; ++q) {
       if (valid[q]) {
-        const double2 *xs = L.x + ((size_t)j * bs + nrow[q]) * R + r0;
+        const size_t xo = ((size_t)j * bs + nrow[q]) * R + r0;
 #pragma unroll
         for (int r = 0; r < RT; ++r) {
-          const double2 xv = xs[r];
-          const Real xr = (Real)xv.x, xim = (Real)xv.y;
+          Real xr, xim;
+          if constexpr (sizeof(Real) == sizeof(float)) {
+            if (L.x32) {
+              const float2 xv = L.x32[xo + r];
+              xr = xv.x;
+              xim = xv.y;
+            } else {
+              const double2 xv = L.x[xo + r];
+              xr = (Real)xv.x;
+              xim = (Real)xv.y;
+            }
+          } else {
+            const double2 xv = L.x[xo + r];
+            xr = (Real)xv.x;
+            xim = (Real)xv.y;
+          }
           cplx u;
           u.x = ph_re[q] * xr - ph_im[q] * xim;
           u.y = ph_re[q] * xim + ph_im[q] * xr;

@@ -1053,6 +1053,11 @@ static void launch_receiver_fp32(sg_context *c, const double2 *x, double2 *y, in
   L.rho_min = c->rho_min;
   L.res = c->res;
   L.x = x;
+  const size_t len = (size_t)c->n * c->bs * R;
+  c->bk_x32.reserve(len);
+  k_to_f32(x, c->bk_x32.ptr, len, st);
+  c->launches += 1;
+  L.x32 = c->bk_x32.ptr;
   L.y = y;
   L.nrhs = R;
   L.master = master ? 1 : 0;
@@ -1118,6 +1123,13 @@ void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool maste
     L.rho_min = c->rho_min;
     L.res = c->res;
     L.x = x;
+    if (fp32) {  // one FP32 copy of the input instead of an FP64->FP32 conversion per pair
+      const size_t len = (size_t)c->n * c->bs * R;
+      c->bk_x32.reserve(len);
+      k_to_f32(x, c->bk_x32.ptr, len, st);
+      c->launches += 1;
+      L.x32 = c->bk_x32.ptr;
+    }
     L.y = y;
     L.nrhs = R;
     L.master = master ? 1 : 0;

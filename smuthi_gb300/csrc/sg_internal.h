@@ -70,6 +70,7 @@ struct CouplingLaunch {
   int n, bs, n_int, ncoef;
   double rho_min, res;
   const double2 *x;     // padded input
+  const float2 *x32;    // FP32 path: FP32 copy of x (read by the emitter loop; null = convert per pair)
   double2 *y;           // padded output (or split partials)
   double2 *partial;     // [nsplit][N][bs][R] scratch when nsplit > 1
   int nrhs;             // R (leading dimension of x, y)
@@ -110,6 +111,7 @@ void build_pairs(const double2 *pos, int n, double rho_min, double res, int n_in
 void k_gather(const double2 *src, double2 *dst, const int *map, int n_unknowns, int nrhs, cudaStream_t st);
 void k_scatter(const double2 *src, double2 *dst, const int *map, int n_unknowns, int nrhs, cudaStream_t st);
 void k_zero(double2 *p, size_t n, cudaStream_t st);
+void k_to_f32(const double2 *x, float2 *y, size_t n, cudaStream_t st);
 
 // FMA-throughput probe (TFLOP/s) of the FP64 or FP32 pipe
 double fma_peak(int fp64, cudaStream_t st);

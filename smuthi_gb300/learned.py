@@ -360,11 +360,11 @@ def main(argv=None):
     ap.add_argument("--shape", default="c5")
     ap.add_argument("--n-train", type=int, default=1000)
     ap.add_argument("--n-val", type=int, default=2000)
-    ap.add_argument("--out", default=None, help="weights name (default film_<shape>)")
+    ap.add_argument("--out", default=None, help="weights name (default precond_<shape>)")
     ap.add_argument("--dir", default=None, help="output directory (default: the package data directory)")
     a = ap.parse_args(argv)
     p, rep = fit_film_weights(a.shape, a.n_train, a.n_val)
-    name = a.out or "film_%s" % a.shape
+    name = a.out or "precond_%s" % a.shape
     path = save_params(p, name, meta={"report": json.dumps(rep, default=float)}, directory=a.dir)
     print(json.dumps(rep, default=float))
     print("wrote", path)

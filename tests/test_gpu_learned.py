@@ -225,7 +225,7 @@ def test_committed_weights_reduce_iterations_on_held_out_film(gpu_context):
     film ensemble none of the training or selection runs saw, at the same FP64-true tolerance."""
     from smuthi_gb300 import learned
     val = learned.film_system("c5", 1000, nrhs=16, seed=31, ctx=gpu_context)
-    weights = learned.load_params("film_c5", val["blocksize"])
+    weights = learned.load_params("precond_c5", val["blocksize"])
     base, rel0 = learned.solve_iterations(val)
     info, rel = learned.solve_iterations(val, weights)
     assert rel0.max() <= 1e-6 and rel.max() <= 1e-6
