@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <type_traits>
+
 #include "sg_df64.h"
 #include "sg_internal.h"
 
@@ -171,6 +173,10 @@ __global__ void __launch_bounds__(kThreads) coupling_kernel(const CouplingLaunch
               xr = (Real)xv.x;
               xim = (Real)xv.y;
             }
+          } else if constexpr (std::is_same<Real, df64>::value) {
+            const df64x2 xv = ldc(reinterpret_cast<const df64x2 *>(L.xdf) + xo + r);
+            xr = xv.x;
+            xim = xv.y;
           } else {
             const double2 xv = L.x[xo + r];
             xr = (Real)xv.x;
@@ -193,27 +199,67 @@ __global__ void __launch_bounds__(kThreads) coupling_kernel(const CouplingLaunch
 #pragma unroll
       for (int r = 0; r < RT; ++r) pa_re[q][r] = pa_im[q][r] = Real(0);
     const cplx *cbase = coef + (size_t)k * NC * bs2;
-    for (int n2 = 0; n2 < bs; ++n2) {
-      cplx u[RT];
+    if constexpr (std::is_same<Real, double>::value) {
+      for (int n2 = 0; n2 < bs; ++n2) {
+        cplx u[RT];
 #pragma unroll
-      for (int r = 0; r < RT; ++r) u[r] = (sizeof(Real) == sizeof(double)) ? ubuf[r * bs + n2] : ubuf[n2 * RT + r];
+        for (int r = 0; r < RT; ++r) u[r] = ubuf[r * bs + n2];
 #pragma unroll
-      for (int q = 0; q < P; ++q) {
-        const cplx *cp = cbase + (size_t)n2 * bs + nrowc[q];
-        cplx cc = ldc(cp + (NC - 1) * bs2);
-        Real lr = cc.x, li = cc.y;
+        for (int q = 0; q < P; ++q) {
+          const cplx *cp = cbase + (size_t)n2 * bs + nrowc[q];
+          cplx cc = ldc(cp + (NC - 1) * bs2);
+          Real lr = cc.x, li = cc.y;
 #pragma unroll
-        for (int ci = NC - 2; ci >= 0; --ci) {
-          const cplx d = ldc(cp + ci * bs2);
-          lr = fma(lr, t, d.x);
-          li = fma(li, t, d.y);
+          for (int ci = NC - 2; ci >= 0; --ci) {
+            const cplx d = ldc(cp + ci * bs2);
+            lr = fma(lr, t, d.x);
+            li = fma(li, t, d.y);
+          }
+#pragma unroll
+          for (int r = 0; r < RT; ++r) {
+            pa_re[q][r] = fma(lr, u[r].x, pa_re[q][r]);
+            pa_re[q][r] = fma(-li, u[r].y, pa_re[q][r]);
+            pa_im[q][r] = fma(lr, u[r].y, pa_im[q][r]);
+            pa_im[q][r] = fma(li, u[r].x, pa_im[q][r]);
+          }
         }
+      }
+    } else {
+      // FP32 and double-float: the coefficient loads are L2-latency bound, so the next column's
+      // coefficients are fetched into registers while the current column is applied (the last
+      // iteration re-reads its own column, which stays in bounds)
+      cplx cf[P][NC];
 #pragma unroll
-        for (int r = 0; r < RT; ++r) {
-          pa_re[q][r] = fma(lr, u[r].x, pa_re[q][r]);
-          pa_re[q][r] = fma(-li, u[r].y, pa_re[q][r]);
-          pa_im[q][r] = fma(lr, u[r].y, pa_im[q][r]);
-          pa_im[q][r] = fma(li, u[r].x, pa_im[q][r]);
+      for (int q = 0; q < P; ++q)
+#pragma unroll
+        for (int ci = 0; ci < NC; ++ci) cf[q][ci] = ldc(cbase + ci * bs2 + nrowc[q]);
+      for (int n2 = 0; n2 < bs; ++n2) {
+        const int n2n = n2 + 1 < bs ? n2 + 1 : n2;
+        cplx nf[P][NC];
+#pragma unroll
+        for (int q = 0; q < P; ++q)
+#pragma unroll
+          for (int ci = 0; ci < NC; ++ci) nf[q][ci] = ldc(cbase + ci * bs2 + (size_t)n2n * bs + nrowc[q]);
+        cplx u[RT];
+#pragma unroll
+        for (int r = 0; r < RT; ++r) u[r] = (sizeof(Real) == sizeof(double)) ? ubuf[r * bs + n2] : ubuf[n2 * RT + r];
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+          Real lr = cf[q][NC - 1].x, li = cf[q][NC - 1].y;
+#pragma unroll
+          for (int ci = NC - 2; ci >= 0; --ci) {
+            lr = fma(lr, t, cf[q][ci].x);
+            li = fma(li, t, cf[q][ci].y);
+          }
+#pragma unroll
+          for (int r = 0; r < RT; ++r) {
+            pa_re[q][r] = fma(lr, u[r].x, pa_re[q][r]);
+            pa_re[q][r] = fma(-li, u[r].y, pa_re[q][r]);
+            pa_im[q][r] = fma(lr, u[r].y, pa_im[q][r]);
+            pa_im[q][r] = fma(li, u[r].x, pa_im[q][r]);
+          }
+#pragma unroll
+          for (int ci = 0; ci < NC; ++ci) cf[q][ci] = nf[q][ci];
         }
       }
     }
@@ -372,6 +418,9 @@ void build_coefficients_df64(const double2 *coef64, void *coefdf, size_t n, cuda
   coef_to_df64_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(coef64, reinterpret_cast<df64x2 *>(coefdf), n);
   SG_CUDA(cudaGetLastError());
 }
+
+// df64x2 copy of an FP64 vector (the double-float kernel's input)
+void k_to_df64(const double2 *x, void *xdf, size_t n, cudaStream_t st) { build_coefficients_df64(x, xdf, n, st); }
 
 int launch_coupling(const CouplingLaunch &L, bool fp32, int nsplit, cudaStream_t st) {
   SG_REQUIRE(L.bs >= 1 && L.bs <= 96, "blocksize must be in [1, 96]");

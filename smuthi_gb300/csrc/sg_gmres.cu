@@ -1175,6 +1175,11 @@ void apply_padded_df64(sg_context *c, const double2 *x, double2 *y, int R, bool 
   L.rho_min = c->rho_min;
   L.res = c->res;
   L.x = x;
+  const size_t len = (size_t)c->n * c->bs * R;
+  c->xdf.reserve(len);
+  k_to_df64(x, c->xdf.ptr, len, st);
+  c->launches += 1;
+  L.xdf = c->xdf.ptr;
   L.y = y;
   L.nrhs = R;
   L.master = master ? 1 : 0;

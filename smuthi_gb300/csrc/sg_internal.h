@@ -71,6 +71,7 @@ struct CouplingLaunch {
   double rho_min, res;
   const double2 *x;     // padded input
   const float2 *x32;    // FP32 path: FP32 copy of x (read by the emitter loop; null = convert per pair)
+  const void *xdf;      // double-float path: df64x2 copy of x (required)
   double2 *y;           // padded output (or split partials)
   double2 *partial;     // [nsplit][N][bs][R] scratch when nsplit > 1
   int nrhs;             // R (leading dimension of x, y)
@@ -85,6 +86,7 @@ int launch_coupling(const CouplingLaunch &L, bool fp32, int nsplit, cudaStream_t
 // the same in double-float arithmetic (L.coef = df64 coefficients from build_coefficients_df64)
 int launch_coupling_df64(const CouplingLaunch &L, int nsplit, cudaStream_t st);
 void build_coefficients_df64(const double2 *coef64, void *coefdf, size_t n, cudaStream_t st);
+void k_to_df64(const double2 *x, void *xdf, size_t n, cudaStream_t st);
 // y = M x or W x in double-float arithmetic (FP64-grade; builds the df64 coefficients on first use)
 void apply_padded_df64(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st);
 // padded-vector operator application and solver (sg_gmres.cu)
@@ -151,6 +153,7 @@ struct sg_context {
   sg::DevBuf<int4> pairs;
   sg::DevBuf<double2> coefdf;  // FP64 coefficients split into two FP32 words each (16 bytes per complex)
   bool df_ready = false;
+  sg::DevBuf<double2> xdf;  // double-float copy of the operator input (16 bytes per complex)
   bool pairs_ready = false;  // FP32 operator data (bucket plan or pair table) is built
 
   // interval-bucketed FP32 operator (sg_bucket.cu)
