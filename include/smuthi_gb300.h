@@ -51,6 +51,10 @@ extern "C" {
  * sg_gmres_solve's precision with SG_FP32, the refinement's true residuals use it in place of the
  * FP64 operator. No counterpart in the reference. */
 #define SG_DF64 8
+/* matvec precision: the FP32-grade operator on the tensor cores (tcgen05.mma kind::tf32, each
+ * operand split into a TF32 high part and a remainder, three products), for blocksize <= 32,
+ * uniform particles, diagonal T and nrhs in {8, 16, 32}. No counterpart in the reference. */
+#define SG_TF32X3 16
 
 typedef struct sg_context sg_context;
 
@@ -136,7 +140,7 @@ int sg_true_residual(sg_context *ctx, const double *b, const double *x, int nrhs
 /* Kernel instrumentation. sg_profile(ctx, 1) brackets every coupling-kernel
  * launch with CUDA events on its stream; sg_kernel_timing synchronises and
  * returns the summed event time (ms) and the number of bracketed launches
- * of the given precision (SG_FP64, SG_FP32, SG_DF64, or -1 for all) since the last
+ * of the given precision (SG_FP64, SG_FP32, SG_DF64, SG_TF32X3, or -1 for all) since the last
  * reset. sg_launch_count returns the number of kernels this context has
  * launched since it was created. */
 int sg_profile(sg_context *ctx, int enable);

@@ -20,6 +20,7 @@ SG_FP64, SG_FP32 = 0, 1
 SG_BLOCK_GMRES = 2  # OR-ed with SG_FP32: block GMRES correction solves
 SG_PRECOND = 4  # OR-ed with SG_FP32: flexible GMRES corrections with the learned preconditioner
 SG_DF64 = 8  # double-float operator; OR-ed with SG_FP32: refinement residuals in double-float
+SG_TF32X3 = 16  # FP32-grade operator on the tensor cores (3xTF32), batched RHS
 KINDS = {"linear": SG_LINEAR, "cubic": SG_CUBIC, "cubic_hermite": SG_CUBIC_HERMITE}
 
 #: every entry point declared in include/smuthi_gb300.h

@@ -265,18 +265,37 @@ static void matvec_dev(sg_context *c, const double2 *x, double2 *y, int R, int p
                        cudaStream_t st) {
   require_ready(c, master);
   SG_REQUIRE(R >= 1 && R <= 256, "nrhs must be in [1, 256]");
-  SG_REQUIRE(precision == SG_FP64 || precision == SG_FP32 || precision == SG_DF64, "unknown precision");
+  SG_REQUIRE(precision == SG_FP64 || precision == SG_FP32 || precision == SG_DF64 || precision == SG_TF32X3,
+             "unknown precision");
   use_device(c);
   const bool fp32 = precision == SG_FP32;
-  if (fp32) ensure_pairs(c, st);
+  if (fp32 || precision == SG_TF32X3) ensure_pairs(c, st);
   const double2 *xp = to_padded(c, x, c->pad_in, R, st);
   double2 *yp = y;
   if (!c->uniform) {
     c->pad_out.reserve(c->padded(R));
     yp = c->pad_out.ptr;
   }
-  if (precision == SG_DF64) sg::apply_padded_df64(c, xp, yp, R, master, st);
-  else sg::apply_padded(c, xp, yp, R, master, fp32, st);
+  if (precision == SG_DF64) {
+    sg::apply_padded_df64(c, xp, yp, R, master, st);
+  } else if (precision == SG_TF32X3) {
+    SG_REQUIRE(sg::tc_supported(c, R),
+               "SG_TF32X3 needs blocksize <= 32, uniform particles, diagonal T and nrhs in {8, 16, 32}");
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (c->profiling) {
+      SG_CUDA(cudaEventCreate(&e0));
+      SG_CUDA(cudaEventCreate(&e1));
+      SG_CUDA(cudaEventRecord(e0, st));
+    }
+    c->launches += sg::launch_tc_matvec(c, xp, yp, R, master, st);
+    if (c->profiling) {
+      SG_CUDA(cudaEventRecord(e1, st));
+      c->events.push_back({e0, e1, 3});
+    }
+    if (sg::tc_check_error(c, st)) throw sg::Error{SG_ERR_CUDA, "tensor-core operator: a bounded wait ran out"};
+  } else {
+    sg::apply_padded(c, xp, yp, R, master, fp32, st);
+  }
   if (!c->uniform) {
     sg::k_scatter(yp, y, c->map.ptr, c->n_unknowns, R, st);
     c->launches += 1;
@@ -435,8 +454,9 @@ int sg_profile(sg_context *ctx, int enable) {
 int sg_kernel_timing(sg_context *ctx, int precision, double *total_ms, int64_t *count, int reset) {
   return guarded([&]() -> int {
     SG_REQUIRE(ctx != nullptr, "null context");
-    SG_REQUIRE(precision == -1 || precision == SG_FP64 || precision == SG_FP32 || precision == SG_DF64,
-               "precision must be SG_FP64, SG_FP32, SG_DF64 or -1 (all)");
+    SG_REQUIRE(precision == -1 || precision == SG_FP64 || precision == SG_FP32 || precision == SG_DF64 ||
+                   precision == SG_TF32X3,
+               "precision must be SG_FP64, SG_FP32, SG_DF64, SG_TF32X3 or -1 (all)");
     use_device(ctx);
     for (auto &ev : ctx->events) {
       SG_CUDA(cudaEventSynchronize(ev.e1));
@@ -448,8 +468,8 @@ int sg_kernel_timing(sg_context *ctx, int precision, double *total_ms, int64_t *
       cudaEventDestroy(ev.e1);
     }
     ctx->events.clear();
-    const int slot = precision == SG_DF64 ? 2 : precision;
-    const int lo = precision < 0 ? 0 : slot, hi = precision < 0 ? 2 : slot;
+    const int slot = precision == SG_DF64 ? 2 : (precision == SG_TF32X3 ? 3 : precision);
+    const int lo = precision < 0 ? 0 : slot, hi = precision < 0 ? 3 : slot;
     double ms = 0.0;
     int64_t n = 0;
     for (int p = lo; p <= hi; ++p) {
@@ -459,8 +479,10 @@ int sg_kernel_timing(sg_context *ctx, int precision, double *total_ms, int64_t *
     if (total_ms) *total_ms = ms;
     if (count) *count = n;
     if (reset) {
-      ctx->coupling_ms[0] = ctx->coupling_ms[1] = ctx->coupling_ms[2] = 0.0;
-      ctx->coupling_launches[0] = ctx->coupling_launches[1] = ctx->coupling_launches[2] = 0;
+      for (int p = 0; p < 4; ++p) {
+        ctx->coupling_ms[p] = 0.0;
+        ctx->coupling_launches[p] = 0;
+      }
     }
     return SG_OK;
   });

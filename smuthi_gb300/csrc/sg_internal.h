@@ -87,6 +87,10 @@ int launch_coupling(const CouplingLaunch &L, bool fp32, int nsplit, cudaStream_t
 int launch_coupling_df64(const CouplingLaunch &L, int nsplit, cudaStream_t st);
 void build_coefficients_df64(const double2 *coef64, void *coefdf, size_t n, cudaStream_t st);
 void k_to_df64(const double2 *x, void *xdf, size_t n, cudaStream_t st);
+// tensor-core (tcgen05, 3xTF32) FP32-grade operator for batched RHS (sg_tc.cu)
+bool tc_supported(const sg_context *c, int R);
+int launch_tc_matvec(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st);
+bool tc_check_error(sg_context *c, cudaStream_t st);  // reads and clears the timeout flag (synchronises)
 // y = M x or W x in double-float arithmetic (FP64-grade; builds the df64 coefficients on first use)
 void apply_padded_df64(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st);
 // padded-vector operator application and solver (sg_gmres.cu)
@@ -154,6 +158,9 @@ struct sg_context {
   sg::DevBuf<double2> coefdf;  // FP64 coefficients split into two FP32 words each (16 bytes per complex)
   bool df_ready = false;
   sg::DevBuf<double2> xdf;  // double-float copy of the operator input (16 bytes per complex)
+  sg::DevBuf<float> tc_xop;  // tensor-core operator: pre-split TF32 hi/lo RHS panels
+  sg::DevBuf<int> tc_err;    // tensor-core operator: set when a bounded wait ran out
+  bool tc_err_init = false;
   bool pairs_ready = false;  // FP32 operator data (bucket plan or pair table) is built
 
   // interval-bucketed FP32 operator (sg_bucket.cu)
@@ -206,8 +213,8 @@ struct sg_context {
     int fp32;
   };
   std::vector<Timed> events;
-  int64_t coupling_launches[3] = {0, 0, 0};  // [fp64, fp32, df64]
-  double coupling_ms[3] = {0.0, 0.0, 0.0};
+  int64_t coupling_launches[4] = {0, 0, 0, 0};  // [fp64, fp32, df64, tf32x3]
+  double coupling_ms[4] = {0.0, 0.0, 0.0, 0.0};
 
   size_t padded(int nrhs) const { return (size_t)n * bs * nrhs; }
 };

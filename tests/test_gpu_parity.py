@@ -268,3 +268,21 @@ def test_mixed_solution_with_df64_residuals(name, gpu_context):
     assert gpu_context.true_residual(B, X).max() <= 1e-6
     for q, k in enumerate(keys):
         assert gc.relerr(X[:, q], g[k]) < 1e-4
+
+
+@pytest.mark.parametrize("name", ["c5s", "c2s", "c1"])
+def test_tensor_core_operator_matches_fp64(name, gpu_context):
+    """The tcgen05 3xTF32 operator is FP32-grade: W x and M x within 2e-6 of the FP64 operator."""
+    from smuthi_gb300 import _lib
+    g = gc.load(name)
+    kind = _kinds(g)[0]
+    parts, ls, wl, W, M = _product_system(g, kind, gpu_context)
+    x = g["x_" + kind]
+    rng = np.random.default_rng(4)
+    for R in (8, 16, 32):
+        X = np.ascontiguousarray(np.stack([x * np.exp(2j * np.pi * rng.random()) * (1 + 0.5 * rng.random())
+                                           for _ in range(R)], axis=1))
+        for fn in (gpu_context.coupling_matvec, gpu_context.master_matvec):
+            ref = fn(X, _lib.SG_FP64)
+            tc = fn(X, _lib.SG_TF32X3)
+            assert gc.relerr(tc, ref) < 2e-6, (R, fn.__name__, gc.relerr(tc, ref))
