@@ -15,7 +15,7 @@ import numpy as np
 
 from . import _lib, learned
 
-PRECISIONS = {"fp64": _lib.SG_FP64, "fp32": _lib.SG_FP32, "df64": _lib.SG_DF64}
+PRECISIONS = {"fp64": _lib.SG_FP64, "fp32": _lib.SG_FP32, "df64": _lib.SG_DF64, "tf32x3": _lib.SG_TF32X3}
 
 
 def main(argv=None):
