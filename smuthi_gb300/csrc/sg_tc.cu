@@ -116,7 +116,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
   constexpr int NN = 2 * R;             // MMA N
   constexpr int ATILE = 128 * kBP;      // floats per A tile (one of hi / lo)
   constexpr int XTILE = NN * kBP;       // floats per x tile
-  constexpr int NCOLS = NN < 32 ? 32 : NN;  // tensor-memory columns (power of two >= 32)
+  // tensor-memory columns: the hi*hi products accumulate in columns [0, NN), the two correction
+  // products (hi*lo, lo*hi, ~2^-11 smaller) in their own accumulator at columns [NN, 2 NN), so the
+  // tensor core's accumulation never adds them to the much larger main sums
+  constexpr int NCOLS = 2 * NN < 32 ? 32 : 2 * NN;
   static_assert(NN == 16 || NN == 32 || NN == 64, "2R must be 16, 32 or 64");
   extern __shared__ __align__(1024) unsigned char tc_smem[];
   float *As = reinterpret_cast<float *>(tc_smem);             // [2 stages][hi, lo][ATILE]
@@ -232,11 +235,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
         for (int prod = 0; prod < 3; ++prod) {
           const uint32_t aa = (prod == 2 ? a_lo : a_hi) + koff;
           const uint32_t bb = (prod == 1 ? x_lo : x_hi) + koff;
-          const uint32_t acc = (jj > 0 || ks > 0 || prod > 0) ? 1u : 0u;
+          const uint32_t acc = (jj > 0 || ks > 0 || prod > 1) ? 1u : 0u;
+          const uint32_t dcol = prod == 0 ? tmem : tmem + (uint32_t)NN;
           asm volatile(
               "{\n\t.reg .pred p;\n\t"
               "setp.ne.b32 p, %4, 0;\n\t"
-              "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+              "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(dcol),
               "l"(tc_desc(aa)), "l"(tc_desc(bb)), "r"(idesc), "r"(acc)
               : "memory");
         }
@@ -259,9 +263,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const bool good = ok && issued == N;
   // epilogue: warps 0-3 read their 32 accumulator lanes into shared memory (the A stages are free)
-  float *Ds = As;  // [128][NN]
-  if (good && warp < 4) {
-    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+  float *Ds = As;  // [128][2 NN]: main sums, then corrections
+  for (int part = 0; part < 2 && good && warp < 4; ++part) {
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(part * NN);
     float v[NN];
     if constexpr (NN == 16) {
       asm volatile(
@@ -288,7 +292,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
     const int row = warp * 32 + lane;
 #pragma unroll
-    for (int c = 0; c < NN; ++c) Ds[row * NN + c] = v[c];
+    for (int c = 0; c < NN; ++c) Ds[row * 2 * NN + part * NN + c] = v[c];
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -300,9 +304,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
   for (int e = tid; e < nrecv * bs * R; e += kTcThreads) {
     const int r = e / (bs * R), rem = e - r * bs * R, n1 = rem / R, c = rem - n1 * R;
     const int i = i0 + r;
-    const float *d0 = Ds + (size_t)(r * 64 + n1) * NN, *d1 = Ds + (size_t)(r * 64 + 32 + n1) * NN;
-    const double yr = (double)d0[c] - (double)d1[R + c];
-    const double yi = (double)d0[R + c] + (double)d1[c];
+    const float *d0 = Ds + (size_t)(r * 64 + n1) * 2 * NN, *d1 = Ds + (size_t)(r * 64 + 32 + n1) * 2 * NN;
+    auto sum = [&](const float *d, int col) { return (double)d[col] + (double)d[NN + col]; };
+    const double yr = sum(d0, c) - sum(d1, R + c);
+    const double yi = sum(d0, R + c) + sum(d1, c);
     const size_t o = ((size_t)i * bs + n1) * R + c;
     if (a.master) {
       const double2 tv = a.t[(size_t)a.ptype[i] * bs + n1];
