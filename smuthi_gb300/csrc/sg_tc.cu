@@ -116,10 +116,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
   constexpr int NN = 2 * R;             // MMA N
   constexpr int ATILE = 128 * kBP;      // floats per A tile (one of hi / lo)
   constexpr int XTILE = NN * kBP;       // floats per x tile
-  // tensor-memory columns: the hi*hi products accumulate in columns [0, NN), the two correction
-  // products (hi*lo, lo*hi, ~2^-11 smaller) in their own accumulator at columns [NN, 2 NN), so the
-  // tensor core's accumulation never adds them to the much larger main sums
-  constexpr int NCOLS = 2 * NN < 32 ? 32 : 2 * NN;
+  // Tensor-memory columns. The hi*hi products accumulate in one accumulator, the two correction
+  // products (hi*lo, lo*hi, ~2^-11 smaller) in another, and even and odd emitters use separate
+  // accumulator pairs: the tensor core's accumulation into tensor memory loses precision roughly
+  // in proportion to the number of instructions accumulated (measured: one accumulator 1.3e-5,
+  // main/correction split 4.4e-6, plus even/odd split 2.2e-6 relative at 60 emitters), so shorter
+  // chains and the FP64 sum of the four accumulators in the epilogue keep it FP32-like.
+  constexpr int NCOLS = 4 * NN;  // 64, 128 or 256
+  static_assert(NCOLS >= 32 && NCOLS <= 256, "tensor-memory columns");
   static_assert(NN == 16 || NN == 32 || NN == 64, "2R must be 16, 32 or 64");
   extern __shared__ __align__(1024) unsigned char tc_smem[];
   float *As = reinterpret_cast<float *>(tc_smem);             // [2 stages][hi, lo][ATILE]
@@ -187,32 +191,45 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
     __syncthreads();  // every thread sees the abort flag and the freed stage
     if (*abort_flag) break;
     float *Ah = As + (size_t)s * 2 * ATILE, *Al = Ah + ATILE;
-    // 2 receivers x 4 row blocks x 8 column blocks = 64 core tiles over 8 warps
-    for (int tile = warp; tile < 64; tile += 8) {
-      const int r = tile >> 5, rb = (tile >> 3) & 3, cb = tile & 7;
-      const int n1 = rb * 8 + l_n1, n2 = cb * 4 + l_n2;
-      if (n1 < bs && n2 < bs) {
-        const int k = pk[buf * 2 + r];
-        const float t = pt[buf * 2 + r];
-        const float2 *cp = a.coef + (size_t)k * NC * bs2 + (size_t)n2 * bs + n1;
-        float2 cc = __ldg(cp + (NC - 1) * bs2);
-        float lr = cc.x, li = cc.y;
+    // 2 receivers x 4 row blocks x 8 column blocks = 64 core tiles over 8 warps; all coefficient
+    // loads of a warp's 8 tiles are issued before any is used (one L2 latency per emitter)
+    {
+      float2 cf[8][NC];
+      int nn1[8], nn2[8], rr[8];
 #pragma unroll
-        for (int ci = NC - 2; ci >= 0; --ci) {
-          const float2 d = __ldg(cp + ci * bs2);
-          lr = fmaf(lr, t, d.x);
-          li = fmaf(li, t, d.y);
+      for (int u = 0; u < 8; ++u) {
+        const int tile = warp + 8 * u;
+        rr[u] = tile >> 5;
+        nn1[u] = ((tile >> 3) & 3) * 8 + l_n1;
+        nn2[u] = (tile & 7) * 4 + l_n2;
+        const bool in = nn1[u] < bs && nn2[u] < bs;
+        const int k = pk[buf * 2 + rr[u]];
+        const float2 *cp = a.coef + (size_t)k * NC * bs2 + (size_t)(in ? nn2[u] : 0) * bs + (in ? nn1[u] : 0);
+#pragma unroll
+        for (int ci = 0; ci < NC; ++ci) cf[u][ci] = __ldg(cp + ci * bs2);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int n1 = nn1[u], n2 = nn2[u], r = rr[u];
+        if (n1 < bs && n2 < bs) {
+          const float t = pt[buf * 2 + r];
+          float lr = cf[u][NC - 1].x, li = cf[u][NC - 1].y;
+#pragma unroll
+          for (int ci = NC - 2; ci >= 0; --ci) {
+            lr = fmaf(lr, t, cf[u][ci].x);
+            li = fmaf(li, t, cf[u][ci].y);
+          }
+          const int dm = a.mofn[n2] - a.mofn[n1];
+          float2 e = ph[(buf * 2 + r) * 33 + (dm < 0 ? -dm : dm)];
+          if (dm < 0) e.y = -e.y;
+          const float wr = lr * e.x - li * e.y, wi = lr * e.y + li * e.x;
+          const float wrh = tf32_hi(wr), wih = tf32_hi(wi);
+          const int row = r * 64 + n1;
+          Ah[tc_off(row, n2)] = wrh;
+          Al[tc_off(row, n2)] = wr - wrh;
+          Ah[tc_off(row + 32, n2)] = wih;
+          Al[tc_off(row + 32, n2)] = wi - wih;
         }
-        const int dm = a.mofn[n2] - a.mofn[n1];
-        float2 e = ph[(buf * 2 + r) * 33 + (dm < 0 ? -dm : dm)];
-        if (dm < 0) e.y = -e.y;
-        const float wr = lr * e.x - li * e.y, wi = lr * e.y + li * e.x;
-        const float wrh = tf32_hi(wr), wih = tf32_hi(wi);
-        const int row = r * 64 + n1;
-        Ah[tc_off(row, n2)] = wrh;
-        Al[tc_off(row, n2)] = wr - wrh;
-        Ah[tc_off(row + 32, n2)] = wih;
-        Al[tc_off(row + 32, n2)] = wi - wih;
       }
     }
     // x_j panel (hi, lo) into stage s
@@ -235,8 +252,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
         for (int prod = 0; prod < 3; ++prod) {
           const uint32_t aa = (prod == 2 ? a_lo : a_hi) + koff;
           const uint32_t bb = (prod == 1 ? x_lo : x_hi) + koff;
-          const uint32_t acc = (jj > 0 || ks > 0 || prod > 1) ? 1u : 0u;
-          const uint32_t dcol = prod == 0 ? tmem : tmem + (uint32_t)NN;
+          const uint32_t acc = (jj > 1 || ks > 0 || prod > 1) ? 1u : 0u;
+          const uint32_t dcol = tmem + (uint32_t)((jj & 1) * 2 * NN + (prod == 0 ? 0 : NN));
           asm volatile(
               "{\n\t.reg .pred p;\n\t"
               "setp.ne.b32 p, %4, 0;\n\t"
@@ -263,8 +280,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const bool good = ok && issued == N;
   // epilogue: warps 0-3 read their 32 accumulator lanes into shared memory (the A stages are free)
-  float *Ds = As;  // [128][2 NN]: main sums, then corrections
-  for (int part = 0; part < 2 && good && warp < 4; ++part) {
+  double *Ds = reinterpret_cast<double *>(As);  // [128][NN] FP64 sum of the accumulators (64 KB at NN = 64)
+  const int nparts = N > 1 ? 4 : 2;  // the odd-emitter accumulators exist only when N > 1
+  for (int part = 0; part < nparts && good && warp < 4; ++part) {
     const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(part * NN);
     float v[NN];
     if constexpr (NN == 16) {
@@ -292,7 +310,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
     const int row = warp * 32 + lane;
 #pragma unroll
-    for (int c = 0; c < NN; ++c) Ds[row * 2 * NN + part * NN + c] = v[c];
+    for (int c = 0; c < NN; ++c) Ds[row * NN + c] = (part ? Ds[row * NN + c] : 0.0) + (double)v[c];
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -304,10 +322,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
   for (int e = tid; e < nrecv * bs * R; e += kTcThreads) {
     const int r = e / (bs * R), rem = e - r * bs * R, n1 = rem / R, c = rem - n1 * R;
     const int i = i0 + r;
-    const float *d0 = Ds + (size_t)(r * 64 + n1) * 2 * NN, *d1 = Ds + (size_t)(r * 64 + 32 + n1) * 2 * NN;
-    auto sum = [&](const float *d, int col) { return (double)d[col] + (double)d[NN + col]; };
-    const double yr = sum(d0, c) - sum(d1, R + c);
-    const double yi = sum(d0, R + c) + sum(d1, c);
+    const double *d0 = Ds + (size_t)(r * 64 + n1) * NN, *d1 = Ds + (size_t)(r * 64 + 32 + n1) * NN;
+    const double yr = d0[c] - d1[R + c];
+    const double yi = d0[R + c] + d1[c];
     const size_t o = ((size_t)i * bs + n1) * R + c;
     if (a.master) {
       const double2 tv = a.t[(size_t)a.ptype[i] * bs + n1];

