@@ -148,10 +148,13 @@ int sg_kernel_timing(sg_context *ctx, int precision, double *total_ms, int64_t *
 int sg_launch_count(sg_context *ctx, int64_t *count);
 
 /* FP32-operator autotuner result for an RHS count: variant 0 = per-receiver kernel, 1 =
- * interval-bucketed kernel, -1 = not tuned yet; with the CUDA-event times (ms) of one run of each.
- * The first FP32 application for a new RHS count times both kernels on the live operands
- * (synchronising the stream) and keeps the faster. No counterpart in the reference. */
-int sg_fp32_autotune(sg_context *ctx, int nrhs, int *variant, double *ms_receiver, double *ms_bucket);
+ * interval-bucketed kernel, -1 = not tuned yet; rhs_tile = the per-receiver kernel's RHS tile per
+ * CTA; with the CUDA-event times (ms) of one run of the best per-receiver tile and of the bucketed
+ * kernel (-1 when it is not a candidate). The first FP32 application for a new RHS count times the
+ * per-receiver kernel at up to three RHS tiles and the bucketed kernel on the live operands
+ * (synchronising the stream) and keeps the fastest. No counterpart in the reference. */
+int sg_fp32_autotune(sg_context *ctx, int nrhs, int *variant, int *rhs_tile, double *ms_receiver,
+                     double *ms_bucket);
 
 /* FMA throughput (TFLOP/s, 2 flops per FMA) of the FP64 or FP32 pipe of the
  * context's device, measured with a dependent-chain probe kernel. Used to

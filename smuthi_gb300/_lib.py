@@ -84,7 +84,7 @@ def _declare(L):
         "sg_kernel_timing": [_P, _I, ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_int64), _I],
         "sg_launch_count": [_P, ctypes.POINTER(ctypes.c_int64)],
         "sg_measure_fma_peak": [_P, _I, ctypes.POINTER(_D)],
-        "sg_fp32_autotune": [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D)],
+        "sg_fp32_autotune": [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D)],
         "sg_coupling_matvec_linear_noalloc": [_I, _I, _P, _I, _P, _I, _D, _D, _P, _P, _P, _I, _P],
         "sg_precond_param_count": [_I],
         "sg_precond_add_graph": [_P, _I, _P, ctypes.POINTER(_I)],
@@ -236,12 +236,15 @@ class Context:
         return out.value
 
     def fp32_autotune(self, nrhs):
-        """(variant, ms per-receiver, ms bucketed) chosen for an RHS count, variant -1 if not tuned."""
+        """(variant, RHS tile, ms best per-receiver tile, ms bucketed) for an RHS count; variant -1 if not
+        tuned yet, ms bucketed -1 when that kernel is not a candidate."""
         v = ctypes.c_int()
+        t = ctypes.c_int()
         a = ctypes.c_double()
         b = ctypes.c_double()
-        check(lib().sg_fp32_autotune(self.h, int(nrhs), ctypes.byref(v), ctypes.byref(a), ctypes.byref(b)))
-        return v.value, a.value, b.value
+        check(lib().sg_fp32_autotune(self.h, int(nrhs), ctypes.byref(v), ctypes.byref(t), ctypes.byref(a),
+                                     ctypes.byref(b)))
+        return v.value, t.value, a.value, b.value
 
     # -- learned preconditioner
     def precond_add_graph(self, nbr):

@@ -499,12 +499,14 @@ int sg_measure_fma_peak(sg_context *ctx, int precision, double *tflops) {
   });
 }
 
-int sg_fp32_autotune(sg_context *ctx, int nrhs, int *variant, double *ms_receiver, double *ms_bucket) {
+int sg_fp32_autotune(sg_context *ctx, int nrhs, int *variant, int *rhs_tile, double *ms_receiver,
+                     double *ms_bucket) {
   return guarded([&]() -> int {
     SG_REQUIRE(ctx && variant, "null argument");
     for (const auto &t : ctx->tuned)
       if (t.nrhs == nrhs) {
         *variant = t.variant;
+        if (rhs_tile) *rhs_tile = t.rt;
         if (ms_receiver) *ms_receiver = t.ms_receiver;
         if (ms_bucket) *ms_bucket = t.ms_bucket;
         return SG_OK;

@@ -374,6 +374,17 @@ static void launch_p(const CouplingLaunch &L, int nsplit, cudaStream_t st) {
 template <typename Real, int NC, bool PAIRS>
 static void launch_r(const CouplingLaunch &L, int nsplit, cudaStream_t st) {
   const int R = L.nrhs;
+  if (L.rt > 0) {  // tile chosen by the autotuner (FP32 path)
+    SG_REQUIRE(R % L.rt == 0, "RHS tile must divide nrhs");
+    if constexpr (std::is_same<Real, float>::value) {
+      if (L.rt == 16) return launch_p<Real, NC, 16, PAIRS>(L, nsplit, st);
+    }
+    if (L.rt == 8) return launch_p<Real, NC, 8, PAIRS>(L, nsplit, st);
+    if (L.rt == 4) return launch_p<Real, NC, 4, PAIRS>(L, nsplit, st);
+    if (L.rt == 2) return launch_p<Real, NC, 2, PAIRS>(L, nsplit, st);
+    if (L.rt == 1) return launch_p<Real, NC, 1, PAIRS>(L, nsplit, st);
+    SG_REQUIRE(false, "unsupported RHS tile");
+  }
   if (R % 8 == 0) launch_p<Real, NC, 8, PAIRS>(L, nsplit, st);
   else if (R % 4 == 0) launch_p<Real, NC, 4, PAIRS>(L, nsplit, st);
   else if (R % 2 == 0) launch_p<Real, NC, 2, PAIRS>(L, nsplit, st);

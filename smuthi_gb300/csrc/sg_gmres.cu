@@ -1040,7 +1040,8 @@ void solve_padded(sg_context *c, const double2 *b, double2 *x, int R, double rto
 // One CUDA-event-timed run of each FP32 kernel on the live operands; the faster one is cached per
 // RHS count. Runs once per (context, nrhs) and synchronises the stream, so it must not be reached
 // inside a stream capture.
-static void launch_receiver_fp32(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st) {
+static void launch_receiver_fp32(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st,
+                                 int rt = 0) {
   CouplingLaunch L{};
   L.pos = c->pos.ptr;
   L.mofn = c->mofn.ptr;
@@ -1060,6 +1061,7 @@ static void launch_receiver_fp32(sg_context *c, const double2 *x, double2 *y, in
   L.x32 = c->bk_x32.ptr;
   L.y = y;
   L.nrhs = R;
+  L.rt = rt;
   L.master = master ? 1 : 0;
   L.t = c->tmat.ptr;
   L.ptype = c->ptype.ptr;
@@ -1073,24 +1075,40 @@ static void launch_receiver_fp32(sg_context *c, const double2 *x, double2 *y, in
 }
 
 static int autotune_fp32(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st) {
-  cudaEvent_t e[4];
-  for (auto &ev : e) SG_CUDA(cudaEventCreate(&ev));
-  // warm both paths once (first launches carry one-time set-up costs), then time one run each
-  launch_receiver_fp32(c, x, y, R, master, st);
-  c->launches += launch_bucket_matvec(c, x, y, R, master, st);
-  SG_CUDA(cudaEventRecord(e[0], st));
-  launch_receiver_fp32(c, x, y, R, master, st);
-  SG_CUDA(cudaEventRecord(e[1], st));
-  SG_CUDA(cudaEventRecord(e[2], st));
-  c->launches += launch_bucket_matvec(c, x, y, R, master, st);
-  SG_CUDA(cudaEventRecord(e[3], st));
-  SG_CUDA(cudaEventSynchronize(e[3]));
-  float ms0 = 0.f, ms1 = 0.f;
-  SG_CUDA(cudaEventElapsedTime(&ms0, e[0], e[1]));
-  SG_CUDA(cudaEventElapsedTime(&ms1, e[2], e[3]));
-  for (auto &ev : e) cudaEventDestroy(ev);
-  const int v = ms1 < ms0 ? 1 : 0;
-  c->tuned.push_back({R, v, ms0, ms1});
+  // candidates: the per-receiver kernel with the three largest RHS tiles that divide R (16 only for
+  // the FP32 path), and the bucketed kernel when its plan exists; each is warmed once (first
+  // launches carry one-time set-up) and timed once with CUDA events on the live operands
+  std::vector<int> tiles;
+  for (int rt : {16, 8, 4, 2, 1})
+    if (R % rt == 0 && tiles.size() < 3) tiles.push_back(rt);
+  cudaEvent_t e0, e1;
+  SG_CUDA(cudaEventCreate(&e0));
+  SG_CUDA(cudaEventCreate(&e1));
+  auto time_it = [&](auto &&launch) {
+    launch();
+    SG_CUDA(cudaEventRecord(e0, st));
+    launch();
+    SG_CUDA(cudaEventRecord(e1, st));
+    SG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    SG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    return ms;
+  };
+  float best_rec = -1.f;
+  int best_rt = tiles.front();
+  for (int rt : tiles) {
+    const float ms = time_it([&] { launch_receiver_fp32(c, x, y, R, master, st, rt); });
+    if (best_rec < 0.f || ms < best_rec) {
+      best_rec = ms;
+      best_rt = rt;
+    }
+  }
+  float ms_bucket = -1.f;
+  if (c->use_bucket) ms_bucket = time_it([&] { c->launches += launch_bucket_matvec(c, x, y, R, master, st); });
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const int v = (ms_bucket >= 0.f && ms_bucket < best_rec) ? 1 : 0;
+  c->tuned.push_back({R, v, best_rt, best_rec, ms_bucket});
   return v;
 }
 
@@ -1101,12 +1119,18 @@ void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool maste
     SG_CUDA(cudaEventCreate(&e1));
     SG_CUDA(cudaEventRecord(e0, st));
   }
-  int variant = 0;
-  if (fp32 && c->use_bucket) {
+  int variant = 0, rt = 0;
+  if (fp32) {
     variant = -1;
     for (const auto &t : c->tuned)
-      if (t.nrhs == R) variant = t.variant;
-    if (variant < 0) variant = autotune_fp32(c, x, y, R, master, st);
+      if (t.nrhs == R) {
+        variant = t.variant;
+        rt = t.rt;
+      }
+    if (variant < 0) {
+      variant = autotune_fp32(c, x, y, R, master, st);
+      rt = c->tuned.back().rt;
+    }
   }
   if (variant == 1) {
     c->launches += launch_bucket_matvec(c, x, y, R, master, st);
@@ -1129,6 +1153,7 @@ void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool maste
       k_to_f32(x, c->bk_x32.ptr, len, st);
       c->launches += 1;
       L.x32 = c->bk_x32.ptr;
+      L.rt = rt;
     }
     L.y = y;
     L.nrhs = R;

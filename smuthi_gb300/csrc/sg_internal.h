@@ -75,6 +75,7 @@ struct CouplingLaunch {
   double2 *y;           // padded output (or split partials)
   double2 *partial;     // [nsplit][N][bs][R] scratch when nsplit > 1
   int nrhs;             // R (leading dimension of x, y)
+  int rt;               // RHS tile per CTA (0 = default choice; the FP32 autotuner sets it)
   int master;           // 0: y = W x; 1: y = x - T W x
   const double2 *t;     // T blocks: diag [types][bs] or full [types][bs][bs]
   const int *ptype;     // [N]
@@ -168,7 +169,8 @@ struct sg_context {
   // FP32 kernel autotuner: per RHS count, the faster of the per-receiver and the bucketed kernel
   struct Tuned {
     int nrhs, variant;  // 0 per-receiver, 1 bucketed
-    float ms_receiver, ms_bucket;
+    int rt;             // per-receiver kernel: RHS tile per CTA
+    float ms_receiver, ms_bucket;  // best per-receiver tile, bucketed (< 0: not a candidate)
   };
   std::vector<Tuned> tuned;
   int bk_T = 0, bk_tiles = 0, bk_S = 0;
