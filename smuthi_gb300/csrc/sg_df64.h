@@ -9,7 +9,7 @@
 // double-word arithmetic", ACM TOMS 44(2), 2017: the absolute error of a sum is a small multiple of
 // 2^-46 (|a| + |b|), which is what an accumulation of many terms needs.
 //
-// On GB300 the FP32 pipe issues 59x the FP64 pipe's FMAs; a df64 FMA costs about 15 FP32
+// On GB300 the FP32 pipe issues 59x the FP64 pipe's FMAs; a df64 FMA costs about 12 FP32
 // instructions, so FP64-grade coupling sums run several times faster in df64 than in FP64.
 #pragma once
 
@@ -71,14 +71,18 @@ __device__ __forceinline__ df64 operator*(df64 a, df64 b) {
   return df_fast_two_sum(p, e);
 }
 
-// a * b + c
+// a * b + c, as compensated accumulation: the high words are added exactly (TwoSum) and every
+// rounding error goes into the low word, which is not renormalised. The low word stays a tiny
+// fraction of the high word over the lengths used here (it grows by at most about one ulp of the
+// high word per call), so the pair remains an accurate unevaluated sum and is accepted as an
+// operand by the operations above; conversion to double adds the two words exactly.
 __device__ __forceinline__ df64 fma(df64 a, df64 b, df64 c) {
   const float p = a.hi * b.hi;
   float e = fmaf(a.hi, b.hi, -p);
   e = fmaf(a.hi, b.lo, e);
   e = fmaf(a.lo, b.hi, e);
   const df64 s = df_two_sum(c.hi, p);
-  return df_fast_two_sum(s.hi, s.lo + (c.lo + e));
+  return df64(s.hi, s.lo + (c.lo + e));
 }
 
 // FP64 complex -> df64 complex (hi = nearest float, lo = nearest float of the remainder)
