@@ -144,7 +144,7 @@ def film_system(name, n_spheres=None, nrhs=16, seed=0, ctx=None, device=0):
     rhs = np.stack([(init.PlaneWave(wl, po, az, pl).swe_coefficients(pos, ls, lm, lm) * tdiag[None, :]).ravel()
                     for (po, az, pl) in waves], axis=1)
     return dict(ctx=ctx, W=W, blocksize=W.blocksize, xy=pos[:, :2].copy(), rhs=np.ascontiguousarray(rhs),
-                spec=spec, n=len(parts))
+                spec=spec, n=len(parts), parts=parts, layer_system=ls, waves=waves, wavelength=wl)
 
 
 # ------------------------------------------------------------------------------------------- training

@@ -1,0 +1,85 @@
+"""Check the chosen (mixed-precision) form against an FP64-grade solution on one workload shape.
+
+    python -m smuthi_gb300.validate --workload c5 --nrhs 16 [--precond auto|none|NAME] [--compare]
+
+Solves the shape's plane-wave right-hand sides with the chosen form (FP32 operator inside FP64
+refinement, double-float residuals, the shipped learned preconditioner) to a relative residual of
+1e-6, then refines the same solutions to 1e-10 and verifies that reference with the FP64 operator.
+Prints one JSON line: solve times and iterations, the FP64-true residuals, and the largest relative
+error of the extinction cross sections of the 1e-6 solutions against the reference
+(`--compare` also solves without the preconditioner).
+"""
+import argparse
+import json
+import os
+import time
+
+import numpy as np
+
+from . import _lib, learned
+
+
+def _solve(system, prec, rtol, x0=None, restart=64):
+    import torch
+    ctx = system["ctx"]
+    dev = torch.device("cuda", ctx.device)
+    rhs = system["rhs"]
+    b = torch.from_numpy(rhs).to(dev)
+    x = torch.zeros_like(b) if x0 is None else torch.from_numpy(np.ascontiguousarray(x0)).to(dev)
+    torch.cuda.synchronize(dev)
+    t = time.perf_counter()
+    info = ctx.gmres_dev(b.data_ptr(), x.data_ptr(), rhs.shape[1], rtol, restart=restart, precision=prec)
+    torch.cuda.synchronize(dev)
+    dt = time.perf_counter() - t
+    xs = np.ascontiguousarray(x.cpu().numpy())
+    rel = ctx.true_residual(rhs, xs)  # FP64 operator
+    d = info.as_dict()
+    d.update(seconds=dt, true_rel_max=float(rel.max()))
+    return xs, d
+
+
+def _extinction(system, x):
+    from . import initial_field as init
+    from .postprocessing import far_field as ff
+    n, bs = system["n"], system["blocksize"]
+    out = []
+    for q, (po, az, pl) in enumerate(system["waves"]):
+        pw = init.PlaneWave(system["wavelength"], po, az, pl)
+        out.append(ff.extinction_cross_section(initial_field=pw, particle_list=system["parts"],
+                                               layer_system=system["layer_system"],
+                                               coefficients=x[:, q].reshape(n, bs)))
+    return np.array(out)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--workload", default="c5")
+    ap.add_argument("--n-spheres", type=int, default=None)
+    ap.add_argument("--nrhs", type=int, default=16)
+    ap.add_argument("--precond", default="auto")
+    ap.add_argument("--compare", action="store_true", help="also solve without the preconditioner")
+    a = ap.parse_args(argv)
+    system = learned.film_system(a.workload, a.n_spheres, nrhs=a.nrhs)
+    bs = system["blocksize"]
+    base = _lib.SG_FP32 | _lib.SG_DF64
+    prec, pname = base, None
+    if a.precond != "none":
+        cand = "precond_%s" % a.workload if a.precond == "auto" else a.precond
+        if os.path.exists(os.path.join(learned.DATA_DIR, cand + ".npz")):
+            learned.use(system, learned.load_params(cand, bs))
+            prec, pname = base | _lib.SG_PRECOND, cand
+    out = {"workload": a.workload, "n_spheres": system["n"], "nrhs": a.nrhs, "preconditioner": pname}
+    x, out["chosen"] = _solve(system, prec, 1e-6)
+    if a.compare and pname:
+        _, out["chosen_without_preconditioner"] = _solve(system, base, 1e-6)
+    xr, out["reference_1e-10"] = _solve(system, base, 1e-10, x0=x)
+    ext, ext_ref = _extinction(system, x), _extinction(system, xr)
+    out["extinction_rel_err_max"] = float(np.max(np.abs(ext - ext_ref) / np.abs(ext_ref)))
+    out["solution_rel_err_max"] = float(max(np.linalg.norm(x[:, q] - xr[:, q]) / np.linalg.norm(xr[:, q])
+                                            for q in range(a.nrhs)))
+    print(json.dumps(out, default=float))
+    system["ctx"].close()
+
+
+if __name__ == "__main__":
+    main()
