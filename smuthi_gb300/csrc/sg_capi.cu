@@ -153,6 +153,7 @@ int sg_set_particles(sg_context *ctx, int n_particles, const double *xy, int n_u
       SG_CUDA(cudaMemcpy(ctx->map.ptr, map.data(), n_unknowns * sizeof(int), cudaMemcpyHostToDevice));
     }
     ctx->pairs_ready = false;
+    ctx->tuned_df.clear();
     ctx->kind = -1;  // the table must be re-uploaded for a new geometry
     ctx->t_ready = false;
     ctx->pgraphs.clear();  // preconditioner graphs belong to the old particles
@@ -205,6 +206,7 @@ int sg_set_lookup(sg_context *ctx, int kind, int len_rho, double rho_min, double
     ctx->res = resolution;
     ctx->pairs_ready = false;
     ctx->df_ready = false;
+    ctx->tuned_df.clear();
     ctx->pgraphs.clear();  // their near-field blocks came from the old table
     ctx->p_active = -1;
     return SG_OK;

@@ -407,6 +407,12 @@ int launch_coupling_df64(const CouplingLaunch &L, int nsplit, cudaStream_t st) {
   SG_REQUIRE(L.bs >= 1 && L.bs <= 96, "blocksize must be in [1, 96]");
   SG_REQUIRE(L.ncoef == 2 || L.ncoef == 4, "bad coefficient count");
   const int R = L.nrhs;
+  if (L.rt == 8) {  // wider RHS tile chosen by the double-float autotuner
+    SG_REQUIRE(R % 8 == 0, "RHS tile must divide nrhs");
+    if (L.ncoef == 2) launch_p<df64, 2, 8, false>(L, nsplit, st);
+    else launch_p<df64, 4, 8, false>(L, nsplit, st);
+    return nsplit > 1 ? 2 : 1;
+  }
   if (L.ncoef == 2) {
     if (R % 4 == 0) launch_p<df64, 2, 4, false>(L, nsplit, st);
     else if (R % 2 == 0) launch_p<df64, 2, 2, false>(L, nsplit, st);

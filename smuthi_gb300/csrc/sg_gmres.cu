@@ -1174,6 +1174,34 @@ void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool maste
   }
 }
 
+static void launch_df64(sg_context *c, const double2 *x, double2 *y, int R, bool master, int rt, cudaStream_t st);
+
+// The double-float kernel's RHS tile (4 or 8): chosen once per RHS count by timing both on the live
+// operands (only when 8 divides R), then cached.
+static int df64_tile(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st) {
+  for (const auto &t : c->tuned_df)
+    if (t.first == R) return t.second;
+  int best = 0;
+  if (R % 8 == 0) {
+    cudaEvent_t e[4];
+    for (auto &ev : e) SG_CUDA(cudaEventCreate(&ev));
+    SG_CUDA(cudaEventRecord(e[0], st));
+    launch_df64(c, x, y, R, master, 0, st);
+    SG_CUDA(cudaEventRecord(e[1], st));
+    SG_CUDA(cudaEventRecord(e[2], st));
+    launch_df64(c, x, y, R, master, 8, st);
+    SG_CUDA(cudaEventRecord(e[3], st));
+    SG_CUDA(cudaEventSynchronize(e[3]));
+    float m0 = 0.f, m1 = 0.f;
+    SG_CUDA(cudaEventElapsedTime(&m0, e[0], e[1]));
+    SG_CUDA(cudaEventElapsedTime(&m1, e[2], e[3]));
+    for (auto &ev : e) cudaEventDestroy(ev);
+    best = m1 < m0 ? 8 : 0;
+  }
+  c->tuned_df.push_back({R, best});
+  return best;
+}
+
 void apply_padded_df64(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st) {
   const size_t ncoef_total = (size_t)c->n_int * c->ncoef * c->bs * c->bs;
   if (!c->df_ready) {
@@ -1182,13 +1210,23 @@ void apply_padded_df64(sg_context *c, const double2 *x, double2 *y, int R, bool 
     c->launches += 1;
     c->df_ready = true;
   }
+  const int rt = df64_tile(c, x, y, R, master, st);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (c->profiling) {
     SG_CUDA(cudaEventCreate(&e0));
     SG_CUDA(cudaEventCreate(&e1));
     SG_CUDA(cudaEventRecord(e0, st));
   }
+  launch_df64(c, x, y, R, master, rt, st);
+  if (c->profiling) {
+    SG_CUDA(cudaEventRecord(e1, st));
+    c->events.push_back({e0, e1, 2});
+  }
+}
+
+static void launch_df64(sg_context *c, const double2 *x, double2 *y, int R, bool master, int rt, cudaStream_t st) {
   CouplingLaunch L{};
+  L.rt = rt;
   L.pos = c->pos.ptr;
   L.mofn = c->mofn.ptr;
   L.coef = c->coefdf.ptr;
@@ -1217,10 +1255,6 @@ void apply_padded_df64(sg_context *c, const double2 *x, double2 *y, int R, bool 
     L.partial = c->w_partial.ptr;
   }
   c->launches += launch_coupling_df64(L, ns, st);
-  if (c->profiling) {
-    SG_CUDA(cudaEventRecord(e1, st));
-    c->events.push_back({e0, e1, 2});
-  }
 }
 
 }  // namespace sg

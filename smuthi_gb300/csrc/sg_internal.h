@@ -7,6 +7,7 @@
 
 #include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/smuthi_gb300.h"
@@ -173,6 +174,7 @@ struct sg_context {
     float ms_receiver, ms_bucket;  // best per-receiver tile, bucketed (< 0: not a candidate)
   };
   std::vector<Tuned> tuned;
+  std::vector<std::pair<int, int>> tuned_df;  // double-float kernel: (nrhs, RHS tile)
   int bk_T = 0, bk_tiles = 0, bk_S = 0;
   sg::DevBuf<int> bk_members, bk_offs;
   sg::DevBuf<int4> bk_rec;
