@@ -177,6 +177,14 @@ int sg_coupling_matvec_linear_noalloc(int device, int n_particles, const void *x
                                       const void *m_of_n, int len_rho, double rho_min, double resolution,
                                       const void *table, const void *x, void *y, int nrhs, void *stream);
 
+/* Bessel factors of the layer-mediated lookup table, the GPU part of the table build (the reference
+ * evaluates scipy.special.jv on the host inside smuthi/linearsystem/particlecoupling/
+ * prepare_lookup.py:343-459): out[n][r][k] = J_n(kappa_k * rho_r) * jac_k for n = 0..nmax
+ * (nmax <= 32). kappa, jac: complex128[nk]; rho: float64[nr]; out: complex128[(nmax+1) * nr * nk];
+ * all device buffers on the context's device. Asynchronous on `stream` (NULL = context stream). */
+int sg_bessel_jac_table(sg_context *ctx, const void *kappa, const void *jac, int nk, const void *rho, int nr,
+                        int nmax, void *out, void *stream);
+
 /* ---------------------------------------------------------------------------------------------
  * Learned preconditioner for the mixed solve (no counterpart in the reference, whose GMRES call
  * at smuthi/linearsystem/linear_system.py:285 is unpreconditioned). A message-passing network on

@@ -518,6 +518,19 @@ int sg_fp32_autotune(sg_context *ctx, int nrhs, int *variant, int *rhs_tile, dou
   });
 }
 
+int sg_bessel_jac_table(sg_context *ctx, const void *kappa, const void *jac, int nk, const void *rho, int nr,
+                        int nmax, void *out, void *stream) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx && kappa && jac && rho && out, "null argument");
+    use_device(ctx);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    sg::bessel_jac_table((const double2 *)kappa, (const double2 *)jac, nk, (const double *)rho, nr, nmax,
+                         (double2 *)out, st);
+    ctx->launches += 1;
+    return SG_OK;
+  });
+}
+
 int sg_precond_param_count(int blocksize) {
   if (blocksize < 1 || blocksize > 64) return -1;
   return sg::precond_param_count(blocksize);

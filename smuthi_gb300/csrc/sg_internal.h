@@ -124,6 +124,10 @@ void k_to_f32(const double2 *x, float2 *y, size_t n, cudaStream_t st);
 // FMA-throughput probe (TFLOP/s) of the FP64 or FP32 pipe
 double fma_peak(int fp64, cudaStream_t st);
 
+// Bessel factors of the layer-mediated lookup table (sg_table.cu)
+void bessel_jac_table(const double2 *kp, const double2 *jac, int nk, const double *rho, int nr, int nmax,
+                      double2 *out, cudaStream_t st);
+
 // ---------------------------------------------------------------- learned preconditioner (sg_precond.cu)
 int precond_param_count(int bs);
 void precond_add_graph(sg_context *c, int k, const int *nbr_host, int *graph_id, cudaStream_t st);

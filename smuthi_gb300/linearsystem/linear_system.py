@@ -68,7 +68,8 @@ def unknown_layout(particle_list):
 class CouplingMatrixRadialLookup(SystemMatrix):
     """Builds the radial lookup table (host FP64) for particles at one height."""
 
-    def __init__(self, vacuum_wavelength, particle_list, layer_system, k_parallel='default', resolution=None):
+    def __init__(self, vacuum_wavelength, particle_list, layer_system, k_parallel='default', resolution=None,
+                 table_context=None):
         z = [p.position[2] for p in particle_list]
         if not all(zz == z[0] for zz in z):
             raise ValueError('radial lookup needs all particles at the same height')
@@ -79,7 +80,7 @@ class CouplingMatrixRadialLookup(SystemMatrix):
         self.resolution = resolution
         self.lookup_table, self.radial_distance_array = look.radial_coupling_lookup_table(
             vacuum_wavelength=vacuum_wavelength, particle_list=particle_list, layer_system=layer_system,
-            k_parallel=k_parallel, resolution=resolution)
+            k_parallel=k_parallel, resolution=resolution, context=table_context)
 
 
 class CouplingMatrixRadialLookupCUDA(CouplingMatrixRadialLookup):
@@ -95,10 +96,11 @@ class CouplingMatrixRadialLookupCUDA(CouplingMatrixRadialLookup):
                  cuda_blocksize=None, interpolator_kind='linear', device=0, context=None):
         if interpolator_kind not in ('linear', 'cubic', 'cubic_hermite'):
             raise ValueError('unknown interpolator_kind %r' % interpolator_kind)
-        CouplingMatrixRadialLookup.__init__(self, vacuum_wavelength, particle_list, layer_system, k_parallel,
-                                            resolution)
-        self.interpolator_kind = interpolator_kind
         self.context = context if context is not None else Context(device)
+        # the table's Bessel factors are evaluated on the same GPU
+        CouplingMatrixRadialLookup.__init__(self, vacuum_wavelength, particle_list, layer_system, k_parallel,
+                                            resolution, table_context=self.context)
+        self.interpolator_kind = interpolator_kind
         self.unknown_particle, self.unknown_n, self.m_of_n, _, _ = unknown_layout(particle_list)
         xy = np.array([p.position[:2] for p in particle_list], dtype=np.float64)
         self.context.set_particles(xy, self.unknown_particle, self.unknown_n, self.blocksize, self.m_of_n)

@@ -92,8 +92,13 @@ def direct_part(k_is, rho, l_max, m_max, rho_min_pair):
     return w
 
 
-def layer_mediated_part(vacuum_wavelength, layer_system, i_s, dz, rho, k_parallel, l_max, m_max):
-    """Layer-mediated coupling table (complex128) [len_rho, B, B]."""
+def layer_mediated_part(vacuum_wavelength, layer_system, i_s, dz, rho, k_parallel, l_max, m_max, context=None):
+    """Layer-mediated coupling table (complex128) [len_rho, B, B].
+
+    With a library ``context`` the Bessel factors J_|dm|(kappa rho) * jac and the contraction with the
+    per-(n1, n2) integrand run on that context's GPU (``sg_bessel_jac_table`` and a complex128 GEMM);
+    without one they are evaluated on the host with scipy, as the reference does.
+    """
     k_is = layer_system.wavenumber(i_s, vacuum_wavelength)
     omega = flds.angular_frequency(vacuum_wavelength)
     kp = np.asarray(k_parallel)
@@ -125,20 +130,39 @@ def layer_mediated_part(vacuum_wavelength, layer_system, i_s, dz, rho, k_paralle
     jac = kp / (kz * k_is)
     wr = np.zeros((len(rho), bs * bs), complex)
     dmat = np.abs(mm[:, None] - mm[None, :])
+    besjac_dev = None
+    if context is not None:
+        import torch
+        dev = torch.device("cuda", context.device)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        kp_d = torch.from_numpy(np.ascontiguousarray(kp, dtype=np.complex128)).to(dev)
+        jac_d = torch.from_numpy(np.ascontiguousarray(jac, dtype=np.complex128)).to(dev)
+        rho_d = torch.from_numpy(np.ascontiguousarray(rho, dtype=np.float64)).to(dev)
+        besjac_dev = torch.empty((2 * m_max + 1, len(rho), len(kp)), dtype=torch.complex128, device=dev)
+        context.bessel_jac_table_dev(kp_d.data_ptr(), jac_d.data_ptr(), len(kp), rho_d.data_ptr(), len(rho),
+                                     2 * m_max, besjac_dev.data_ptr(), stream=stream)
     for dm in range(2 * m_max + 1):
         n1s, n2s = np.nonzero(dmat == dm)
         if len(n1s) == 0:
             continue
         belbe = np.einsum('pcak,pcak->ak', X[:, :, n1s, :], Bn[:, :, n2s, :])  # [pairs, k]
         G = (belbe * wts[None, :]).T  # [k, pairs]
-        besjac = scipy.special.jv(dm, kp[None, :] * rho[:, None]) * jac[None, :]
-        wr[:, n1s * bs + n2s] = 2 * ipow(dm) * (besjac @ G)
+        if besjac_dev is not None:
+            Gd = torch.from_numpy(np.ascontiguousarray(G)).to(dev)
+            wr[:, n1s * bs + n2s] = 2 * ipow(dm) * (besjac_dev[dm] @ Gd).cpu().numpy()
+        else:
+            besjac = scipy.special.jv(dm, kp[None, :] * rho[:, None]) * jac[None, :]
+            wr[:, n1s * bs + n2s] = 2 * ipow(dm) * (besjac @ G)
     return wr.reshape(len(rho), bs, bs)
 
 
 def radial_coupling_lookup_table(vacuum_wavelength, particle_list, layer_system, k_parallel='default',
-                                 resolution=None):
-    """Return (lookup_table[rho, n1, n2], rho_grid) for particles at a common height."""
+                                 resolution=None, context=None):
+    """Return (lookup_table[rho, n1, n2], rho_grid) for particles at a common height.
+
+    ``context``: a library context whose GPU evaluates the Bessel factors of the layer-mediated part
+    (None: host scipy, the reference's arithmetic).
+    """
     if resolution is None:
         resolution = vacuum_wavelength / 100
         sys.stdout.write('Setting lookup resolution to %f\n' % resolution)
@@ -157,5 +181,6 @@ def radial_coupling_lookup_table(vacuum_wavelength, particle_list, layer_system,
         k_parallel = flds.default_Sommerfeld_k_parallel_array
     if k_parallel is None:
         raise ValueError('no Sommerfeld contour: pass k_parallel or set the default contour')
-    wr = layer_mediated_part(vacuum_wavelength, layer_system, i_s, dz, rho, k_parallel, l_max, m_max)
+    wr = layer_mediated_part(vacuum_wavelength, layer_system, i_s, dz, rho, k_parallel, l_max, m_max,
+                             context=context)
     return w + wr, rho
