@@ -133,8 +133,9 @@ __global__ void bessel_jac_kernel(const double2 *kp, const double2 *jac, int nk,
     if (az <= 25.0) {
       norm = cdiv(cz{1.0, 0.0}, S);
     } else {
-      // scale by whichever of J_0, J_1 the recurrence found larger (they never vanish together)
-      const bool use1 = cabs2(J[1]) > cabs2(J[0]);
+      // scale by whichever of J_0, J_1 the recurrence found larger (they never vanish together); the
+      // recurrence values can be ~1e-260 here, so compare 1-norms (their squares would underflow)
+      const bool use1 = fabs(J[1].x) + fabs(J[1].y) > fabs(J[0].x) + fabs(J[0].y);
       const cz exact = bessel_j01_asym(use1 ? 1 : 0, z);
       norm = cdiv(exact, use1 ? J[1] : J[0]);
     }
