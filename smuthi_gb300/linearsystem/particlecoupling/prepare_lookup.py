@@ -95,9 +95,10 @@ def direct_part(k_is, rho, l_max, m_max, rho_min_pair):
 def layer_mediated_part(vacuum_wavelength, layer_system, i_s, dz, rho, k_parallel, l_max, m_max, context=None):
     """Layer-mediated coupling table (complex128) [len_rho, B, B].
 
-    With a library ``context`` the Bessel factors J_|dm|(kappa rho) * jac and the contraction with the
-    per-(n1, n2) integrand run on that context's GPU (``sg_bessel_jac_table`` and a complex128 GEMM);
-    without one they are evaluated on the host with scipy, as the reference does.
+    With a library ``context`` the Bessel factors J_|dm|(kappa rho) * jac (the dominant cost of the
+    build) are evaluated on that context's GPU by ``sg_bessel_jac_table``; without one on the host with
+    scipy, as the reference does. The contraction with the per-(n1, n2) integrand is a small FP64 GEMM
+    on the host in both cases (a library FP64 GEMM on the device may use reduced-precision emulation).
     """
     k_is = layer_system.wavenumber(i_s, vacuum_wavelength)
     omega = flds.angular_frequency(vacuum_wavelength)
@@ -130,7 +131,7 @@ def layer_mediated_part(vacuum_wavelength, layer_system, i_s, dz, rho, k_paralle
     jac = kp / (kz * k_is)
     wr = np.zeros((len(rho), bs * bs), complex)
     dmat = np.abs(mm[:, None] - mm[None, :])
-    besjac_dev = None
+    besjac_host = None
     if context is not None:
         import torch
         dev = torch.device("cuda", context.device)
@@ -141,15 +142,16 @@ def layer_mediated_part(vacuum_wavelength, layer_system, i_s, dz, rho, k_paralle
         besjac_dev = torch.empty((2 * m_max + 1, len(rho), len(kp)), dtype=torch.complex128, device=dev)
         context.bessel_jac_table_dev(kp_d.data_ptr(), jac_d.data_ptr(), len(kp), rho_d.data_ptr(), len(rho),
                                      2 * m_max, besjac_dev.data_ptr(), stream=stream)
+        besjac_host = besjac_dev.cpu().numpy()
+        del besjac_dev, kp_d, jac_d, rho_d
     for dm in range(2 * m_max + 1):
         n1s, n2s = np.nonzero(dmat == dm)
         if len(n1s) == 0:
             continue
         belbe = np.einsum('pcak,pcak->ak', X[:, :, n1s, :], Bn[:, :, n2s, :])  # [pairs, k]
         G = (belbe * wts[None, :]).T  # [k, pairs]
-        if besjac_dev is not None:
-            Gd = torch.from_numpy(np.ascontiguousarray(G)).to(dev)
-            wr[:, n1s * bs + n2s] = 2 * ipow(dm) * (besjac_dev[dm] @ Gd).cpu().numpy()
+        if besjac_host is not None:
+            wr[:, n1s * bs + n2s] = 2 * ipow(dm) * (besjac_host[dm] @ G)
         else:
             besjac = scipy.special.jv(dm, kp[None, :] * rho[:, None]) * jac[None, :]
             wr[:, n1s * bs + n2s] = 2 * ipow(dm) * (besjac @ G)
