@@ -64,7 +64,8 @@ const char *sg_last_error(void);
 /* Library version string. */
 const char *sg_version(void);
 
-/* Create / destroy a context on CUDA device `device`.
+/* Create / destroy a context on CUDA device `device`. The context owns a blocking CUDA stream
+ * (ordered with the legacy default stream); a NULL stream argument below means that stream.
  * Replaces the PyCUDA autoinit + gpuarray set-up of
  * smuthi/linearsystem/linear_system.py:829-882. */
 int sg_create(int device, sg_context **out);

@@ -83,7 +83,9 @@ int sg_create(int device, sg_context **out) {
     SG_CUDA(cudaSetDevice(device));
     sg_context *c = new sg_context();
     c->device = device;
-    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    // a blocking stream: work on it is ordered with the legacy default stream, so callers that queue
+    // their inputs there (and pass NULL for "the context's stream") need no extra synchronisation
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamDefault);
     if (e != cudaSuccess) {
       delete c;
       throw sg::Error{SG_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)};
