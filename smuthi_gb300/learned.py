@@ -321,8 +321,9 @@ def evaluate_loss(system, params, pool, batches=8, batch=16, k=K_NEIGHBOURS):
 def fit_film_weights(name="c5", n_train=1000, n_val=2000, seed_train=11, seed_val=12, k=K_NEIGHBOURS, log=print):
     """Train candidate weights for a workload shape and keep the one with the fewest held-out iterations.
 
-    Candidates: the Neumann start; the per-layer alphas trained on the Frobenius objective; full
-    networks fine-tuned from those alphas at two learning rates. Selection is by the FGMRES iteration
+    Candidates: the Neumann start; the per-layer alphas trained on white pairs (the Frobenius
+    objective) or on mostly-Krylov pairs of solved plane waves; full networks fine-tuned from each
+    at two learning rates. Selection is by the FGMRES iteration
     count of the mixed solve of 16 plane waves on a held-out particle set (``n_val`` spheres,
     another seed), because a lower training loss does not by itself mean fewer iterations.
     Returns (best params, report dict).
@@ -334,10 +335,13 @@ def fit_film_weights(name="c5", n_train=1000, n_val=2000, seed_train=11, seed_va
     report = {"shape": name, "n_train": n_train, "n_val": n_val, "k": k, "val_unpreconditioned": base}
     log("unpreconditioned: %d iterations" % base["iterations"])
     cands = {"neumann": init_params(bs)}
-    pool = TrainingPool(tr, white_fraction=1.0, seed=1)
-    cands["alpha"], _ = train(tr, cands["neumann"], steps=300, lr=1e-2, k=k, pool=pool, mask=alpha_mask(bs))
-    for lr in (1e-5, 3e-5):
-        cands["full_%g" % lr], _ = train(tr, cands["alpha"], steps=400, lr=lr, k=k, pool=pool)
+    pools = {"white": TrainingPool(tr, white_fraction=1.0, seed=1),
+             "krylov": TrainingPool(tr, white_fraction=0.25, seed=2)}
+    for pname, pool in pools.items():
+        a_p, _ = train(tr, cands["neumann"], steps=300, lr=1e-2, k=k, pool=pool, mask=alpha_mask(bs))
+        cands["alpha_" + pname] = a_p
+        for lr in (1e-5, 3e-5):
+            cands["full_%s_%g" % (pname, lr)], _ = train(tr, a_p, steps=400, lr=lr, k=k, pool=pool)
     best, best_it = None, None
     for tag, p in cands.items():
         info, rel = solve_iterations(val, p, k=k)
