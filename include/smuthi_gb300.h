@@ -186,6 +186,19 @@ int sg_coupling_matvec_linear_noalloc(int device, int n_particles, const void *x
 int sg_bessel_jac_table(sg_context *ctx, const void *kappa, const void *jac, int nk, const void *rho, int nr,
                         int nmax, void *out, void *stream);
 
+/* Particle sum of the scattered field's plane-wave expansion for the cross sections (the reference
+ * converts each particle's expansion on the host: smuthi/postprocessing/far_field.py:363-427,
+ * smuthi/postprocessing/scattered_field.py:80-150, smuthi/fields/transformations.py:133-233):
+ *   out[r][p][k][a] = sum_i exp(-i kpar_k (cos alpha_a x_i + sin alpha_a y_i))
+ *                     sum_n coef[i][n][r] S[n][p][k] exp(i m_of_n[n] alpha_a)
+ * Device buffers: xy double2[n_particles], coef complex128[n_particles][blocksize][nrhs],
+ * kpar float64[nk] (real), S complex128[blocksize][2][nk], alpha float64[na],
+ * out complex128[nrhs][2][nk][na]; m_of_n is a host array int32[blocksize] with |m| <= m_max <= 16.
+ * FP64 throughout. Synchronous on `stream` (NULL = the context's stream). */
+int sg_farfield_sum(sg_context *ctx, int n_particles, const void *xy, int blocksize, int nrhs, const void *coef,
+                    int m_max, const int32_t *m_of_n, int nk, const void *kpar, const void *S, int na,
+                    const void *alpha, void *out, void *stream);
+
 /* ---------------------------------------------------------------------------------------------
  * Learned preconditioner for the mixed solve (no counterpart in the reference, whose GMRES call
  * at smuthi/linearsystem/linear_system.py:285 is unpreconditioned). A message-passing network on

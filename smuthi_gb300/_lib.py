@@ -30,7 +30,8 @@ EXPORTS = ("sg_last_error", "sg_version", "sg_create", "sg_destroy", "sg_set_par
            "sg_kernel_timing", "sg_launch_count", "sg_measure_fma_peak", "sg_fp32_autotune",
            "sg_coupling_matvec_linear_noalloc", "sg_precond_param_count", "sg_precond_add_graph",
            "sg_precond_select", "sg_precond_clear", "sg_precond_set_params", "sg_precond_get_params",
-           "sg_precond_apply_dev", "sg_precond_train_step", "sg_precond_export_blocks", "sg_bessel_jac_table")
+           "sg_precond_apply_dev", "sg_precond_train_step", "sg_precond_export_blocks", "sg_bessel_jac_table",
+           "sg_farfield_sum")
 
 
 class LibraryMissing(RuntimeError):
@@ -87,6 +88,7 @@ def _declare(L):
         "sg_fp32_autotune": [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D)],
         "sg_coupling_matvec_linear_noalloc": [_I, _I, _P, _I, _P, _I, _D, _D, _P, _P, _P, _I, _P],
         "sg_bessel_jac_table": [_P, _P, _P, _I, _P, _I, _I, _P, _P],
+        "sg_farfield_sum": [_P, _I, _P, _I, _I, _P, _I, _P, _I, _P, _P, _I, _P, _P, _P],
         "sg_precond_param_count": [_I],
         "sg_precond_add_graph": [_P, _I, _P, ctypes.POINTER(_I)],
         "sg_precond_select": [_P, _I],
@@ -291,6 +293,14 @@ class Context:
         check(lib().sg_bessel_jac_table(self.h, ctypes.c_void_p(kappa_ptr), ctypes.c_void_p(jac_ptr), int(nk),
                                         ctypes.c_void_p(rho_ptr), int(nr), int(nmax), ctypes.c_void_p(out_ptr),
                                         ctypes.c_void_p(stream or 0)))
+
+    def farfield_sum_dev(self, n, xy_ptr, bs, nrhs, coef_ptr, m_max, m_of_n, nk, kpar_ptr, S_ptr, na, alpha_ptr,
+                         out_ptr, stream=None):
+        mo = np.ascontiguousarray(m_of_n, dtype=np.int32)
+        check(lib().sg_farfield_sum(self.h, int(n), ctypes.c_void_p(xy_ptr), int(bs), int(nrhs),
+                                    ctypes.c_void_p(coef_ptr), int(m_max), ptr(mo), int(nk), ctypes.c_void_p(kpar_ptr),
+                                    ctypes.c_void_p(S_ptr), int(na), ctypes.c_void_p(alpha_ptr),
+                                    ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream or 0)))
 
     def launch_count(self):
         n = ctypes.c_int64()

@@ -533,6 +533,20 @@ int sg_bessel_jac_table(sg_context *ctx, const void *kappa, const void *jac, int
   });
 }
 
+int sg_farfield_sum(sg_context *ctx, int n_particles, const void *xy, int blocksize, int nrhs, const void *coef,
+                    int m_max, const int32_t *m_of_n, int nk, const void *kpar, const void *S, int na,
+                    const void *alpha, void *out, void *stream) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx && xy && coef && m_of_n && kpar && S && alpha && out, "null argument");
+    use_device(ctx);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    sg::farfield_sum((const double2 *)xy, n_particles, blocksize, nrhs, (const double2 *)coef, m_max, m_of_n, nk,
+                     (const double *)kpar, (const double2 *)S, na, (const double *)alpha, (double2 *)out, st);
+    ctx->launches += 1;
+    return SG_OK;
+  });
+}
+
 int sg_precond_param_count(int blocksize) {
   if (blocksize < 1 || blocksize > 64) return -1;
   return sg::precond_param_count(blocksize);

@@ -128,6 +128,11 @@ double fma_peak(int fp64, cudaStream_t st);
 void bessel_jac_table(const double2 *kp, const double2 *jac, int nk, const double *rho, int nr, int nmax,
                       double2 *out, cudaStream_t st);
 
+// particle sum of the scattered plane-wave expansion (sg_farfield.cu); synchronous
+void farfield_sum(const double2 *xy, int n, int bs, int nrhs, const double2 *coef, int mmax, const int *mofn_host,
+                  int nk, const double *kpar, const double2 *S, int na, const double *alpha, double2 *out,
+                  cudaStream_t st);
+
 // ---------------------------------------------------------------- learned preconditioner (sg_precond.cu)
 int precond_param_count(int bs);
 void precond_add_graph(sg_context *c, int k, const int *nbr_host, int *graph_id, cudaStream_t st);

@@ -31,10 +31,12 @@ def _particle_data(particle_list, coefficients=None):
 
 
 def scattered_pwe(vacuum_wavelength, layer_system, xy, z, l_max, m_max, coefs, layer_number, kpar, alpha,
-                  chunk=16):
+                  chunk=16, context=None):
     """(g_up, g_down) [nrhs, 2, K, A] of the scattered field in ``layer_number``.
 
-    coefs: [nrhs, N, blocksize] outgoing SWE coefficients (or [N, blocksize]).
+    coefs: [nrhs, N, blocksize] outgoing SWE coefficients (or [N, blocksize]). With a library
+    ``context`` (and real ``kpar``) the particle sum runs on that context's GPU (``sg_farfield_sum``,
+    FP64); the angular factors and the layer response stay on the host.
     """
     coefs = np.asarray(coefs)
     single = coefs.ndim == 2
@@ -51,6 +53,17 @@ def scattered_pwe(vacuum_wavelength, layer_system, xy, z, l_max, m_max, coefs, l
     tau, ll, mm = flds.index_table(l_max, m_max)
     nm = 2 * m_max + 1
     gs = []
+    if context is not None:
+        import torch
+        if np.iscomplexobj(kpar) and np.any(np.imag(kpar) != 0):
+            raise ValueError('the GPU far-field sum needs real in-plane wavenumbers')
+        dev = torch.device("cuda", context.device)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        N = coefs.shape[1]
+        c_d = torch.from_numpy(np.ascontiguousarray(np.transpose(coefs, (1, 2, 0)), dtype=np.complex128)).to(dev)
+        xy_d = torch.from_numpy(np.ascontiguousarray(xy, dtype=np.float64)).to(dev)
+        kp_d = torch.from_numpy(np.ascontiguousarray(np.real(kpar), dtype=np.float64)).to(dev)
+        al_d = torch.from_numpy(np.ascontiguousarray(alpha, dtype=np.float64)).to(dev)
     for sgn in (1, -1):  # up, down
         _, pilm, taulm = legendre_normalized(sgn * kz / k, kpar / k, l_max)
         # S[n, pol, K, m]: angular coefficient, nonzero only for m == m(n)
@@ -58,6 +71,16 @@ def scattered_pwe(vacuum_wavelength, layer_system, xy, z, l_max, m_max, coefs, l
         for n in range(len(tau)):
             for pol in range(2):
                 S[n, pol, :, mm[n] + m_max] = transformation_coefficients_vwf(tau[n], ll[n], mm[n], pol, pilm, taulm)
+        pref = np.exp(1j * sgn * kz * dz) / (2 * np.pi * kz * k)
+        if context is not None:
+            Sn = np.ascontiguousarray(S[np.arange(len(tau)), :, :, mm + m_max])  # [n, pol, K]
+            S_d = torch.from_numpy(Sn).to(dev)
+            out = torch.empty((R, 2, len(kpar), len(alpha)), dtype=torch.complex128, device=dev)
+            context.farfield_sum_dev(N, xy_d.data_ptr(), len(tau), R, c_d.data_ptr(), m_max, mm, len(kpar),
+                                     kp_d.data_ptr(), S_d.data_ptr(), len(alpha), al_d.data_ptr(), out.data_ptr(),
+                                     stream=stream)
+            gs.append(out.cpu().numpy() * pref[None, None, :, None])
+            continue
         D = np.einsum('rin,npkm->rpkmi', coefs, S)  # [R, 2, K, m, N]
         eima = np.exp(1j * np.outer(np.arange(-m_max, m_max + 1), alpha))  # [m, A]
         g = np.zeros((R, 2, len(kpar), len(alpha)), complex)
@@ -69,7 +92,6 @@ def scattered_pwe(vacuum_wavelength, layer_system, xy, z, l_max, m_max, coefs, l
             # sum over particles, then over m
             F = np.einsum('kai,rpkmi->rpkam', ph, D[:, :, ks])
             g[:, :, ks, :] = np.einsum('rpkam,ma->rpka', F, eima)
-        pref = np.exp(1j * sgn * kz * dz) / (2 * np.pi * kz * k)
         gs.append(g * pref[None, None, :, None])
     g_up, g_dn = gs
     out_up = np.zeros_like(g_up)
@@ -97,8 +119,9 @@ def _incidence(initial_field, layer_system):
 
 
 def extinction_cross_section(simulation=None, initial_field=None, particle_list=None, layer_system=None,
-                             coefficients=None):
-    """Extinction cross section (top plus bottom extinction) of a plane wave."""
+                             coefficients=None, context=None):
+    """Extinction cross section (top plus bottom extinction) of a plane wave (``context``: GPU particle
+    sum, see ``scattered_pwe``)."""
     initial_field = initial_field or simulation.initial_field
     particle_list = particle_list or simulation.particle_list
     layer_system = layer_system or simulation.layer_system
@@ -119,8 +142,8 @@ def extinction_cross_section(simulation=None, initial_field=None, particle_list=
     rvec = np.array([0, 0, layer_system.reference_z(i_P)]) - np.array(initial_field.reference_point)
     A_P = initial_field.amplitude * np.exp(1j * np.dot(kvec, rvec))
     I0 = abs(A_P) ** 2 * n_P / 2
-    g_top, _ = scattered_pwe(lam, layer_system, xy, z, l_max, m_max, coefs, i_top, kappa, alpha)
-    _, g_bot = scattered_pwe(lam, layer_system, xy, z, l_max, m_max, coefs, 0, kappa, alpha)
+    g_top, _ = scattered_pwe(lam, layer_system, xy, z, l_max, m_max, coefs, i_top, kappa, alpha, context=context)
+    _, g_bot = scattered_pwe(lam, layer_system, xy, z, l_max, m_max, coefs, 0, kappa, alpha, context=context)
     _, init_bot = initial_field.plane_wave_expansion(layer_system, 0)
     init_top, _ = initial_field.plane_wave_expansion(layer_system, i_top)
     kz_bot = flds.k_z(k_parallel=kappa, k=k_bot)
@@ -132,8 +155,9 @@ def extinction_cross_section(simulation=None, initial_field=None, particle_list=
 
 def total_scattering_cross_section(simulation=None, initial_field=None, particle_list=None, layer_system=None,
                                    polar_angles='default', azimuthal_angles='default', angular_resolution=None,
-                                   coefficients=None):
-    """Angle-integrated scattering cross section (trapezoidal rule over the far-field grid)."""
+                                   coefficients=None, context=None):
+    """Angle-integrated scattering cross section (trapezoidal rule over the far-field grid;
+    ``context``: GPU particle sum, see ``scattered_pwe``)."""
     initial_field = initial_field or simulation.initial_field
     particle_list = particle_list or simulation.particle_list
     layer_system = layer_system or simulation.layer_system
@@ -156,7 +180,7 @@ def total_scattering_cross_section(simulation=None, initial_field=None, particle
         if len(sel) <= 1 or np.imag(n_l) != 0:
             continue
         kp = np.sort(np.sin(sel) * n_l) * omega
-        gu, gd = scattered_pwe(lam, layer_system, xy, z, l_max, m_max, coefs, layer, kp, az)
+        gu, gd = scattered_pwe(lam, layer_system, xy, z, l_max, m_max, coefs, layer, kp, az, context=context)
         g = gu if up else gd
         k = omega * n_l
         polar = np.arcsin(kp / k) if up else np.pi - np.arcsin(kp / k)
