@@ -6,8 +6,9 @@ Solves the shape's plane-wave right-hand sides with the chosen form (FP32 operat
 refinement, double-float residuals, the shipped learned preconditioner) to a relative residual of
 1e-6, then refines the same solutions to 1e-10 and verifies that reference with the FP64 operator.
 Prints one JSON line: solve times and iterations, the FP64-true residuals, and the largest relative
-error of the extinction cross sections of the 1e-6 solutions against the reference
-(`--compare` also solves without the preconditioner).
+error of the extinction cross sections (and with `--sca` of the total scattering cross sections,
+whose particle sums run on the GPU) of the 1e-6 solutions against the reference (`--compare` also
+solves without the preconditioner).
 """
 import argparse
 import json
@@ -38,16 +39,20 @@ def _solve(system, prec, rtol, x0=None, restart=64):
     return xs, d
 
 
-def _extinction(system, x):
+def _cross_sections(system, x, which):
+    """Extinction (host) or total scattering (GPU particle sum) cross section per right-hand side."""
     from . import initial_field as init
     from .postprocessing import far_field as ff
     n, bs = system["n"], system["blocksize"]
     out = []
     for q, (po, az, pl) in enumerate(system["waves"]):
         pw = init.PlaneWave(system["wavelength"], po, az, pl)
-        out.append(ff.extinction_cross_section(initial_field=pw, particle_list=system["parts"],
-                                               layer_system=system["layer_system"],
-                                               coefficients=x[:, q].reshape(n, bs)))
+        kw = dict(initial_field=pw, particle_list=system["parts"], layer_system=system["layer_system"],
+                  coefficients=x[:, q].reshape(n, bs))
+        if which == "ext":
+            out.append(ff.extinction_cross_section(**kw))
+        else:
+            out.append(ff.total_scattering_cross_section(context=system["ctx"], **kw))
     return np.array(out)
 
 
@@ -60,6 +65,7 @@ def main(argv=None):
     ap.add_argument("--compare", action="store_true", help="also solve without the preconditioner")
     ap.add_argument("--restart", type=int, default=64, help="GMRES restart length of the 1e-6 solves")
     ap.add_argument("--no-reference", action="store_true", help="skip the 1e-10 reference and cross sections")
+    ap.add_argument("--sca", action="store_true", help="also compare total scattering cross sections (GPU)")
     a = ap.parse_args(argv)
     system = learned.film_system(a.workload, a.n_spheres, nrhs=a.nrhs)
     bs = system["blocksize"]
@@ -89,8 +95,13 @@ def main(argv=None):
         system["ctx"].close()
         return
     xr, out["reference_1e-10"] = _solve(system, base, 1e-10, x0=x)
-    ext, ext_ref = _extinction(system, x), _extinction(system, xr)
+    ext, ext_ref = _cross_sections(system, x, "ext"), _cross_sections(system, xr, "ext")
     out["extinction_rel_err_max"] = float(np.max(np.abs(ext - ext_ref) / np.abs(ext_ref)))
+    if a.sca:
+        t = time.perf_counter()
+        sca, sca_ref = _cross_sections(system, x, "sca"), _cross_sections(system, xr, "sca")
+        out["scattering_rel_err_max"] = float(np.max(np.abs(sca - sca_ref) / np.abs(sca_ref)))
+        out["scattering_seconds"] = time.perf_counter() - t
     out["solution_rel_err_max"] = float(max(np.linalg.norm(x[:, q] - xr[:, q]) / np.linalg.norm(xr[:, q])
                                             for q in range(a.nrhs)))
     print(json.dumps(out, default=float))
