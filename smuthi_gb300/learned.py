@@ -98,6 +98,16 @@ def save_params(params, name, meta=None, directory=None):
     return path
 
 
+def load_meta(name):
+    """Metadata stored with a weights file: {'k': neighbours (default K_NEIGHBOURS), 'report': dict}."""
+    import json
+    d = np.load(os.path.join(DATA_DIR, name + ".npz"))
+    out = {"k": int(d["k"]) if "k" in d.files else K_NEIGHBOURS}
+    if "report" in d.files:
+        out["report"] = json.loads(str(d["report"]))
+    return out
+
+
 def load_params(name, blocksize):
     path = os.path.join(DATA_DIR, name + ".npz")
     d = np.load(path)
