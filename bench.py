@@ -158,7 +158,8 @@ def run_ours(args, rank, world, local_rank):
         cand = "precond_%s" % args.workload if args.precond == "auto" else args.precond
         if os.path.exists(os.path.join(learned.DATA_DIR, cand + ".npz")):
             pname = cand
-            learned.attach(ctx, np.array([p.position[:2] for p in wl["parts"]]), bs, learned.load_params(cand, bs))
+            learned.attach(ctx, np.array([p.position[:2] for p in wl["parts"]]), bs, learned.load_params(cand, bs),
+                           k=learned.load_meta(cand)["k"])
             prec |= _lib.SG_PRECOND
         elif args.precond != "auto":
             raise SystemExit("no shipped preconditioner weights named %r" % cand)

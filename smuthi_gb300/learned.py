@@ -364,6 +364,16 @@ def fit_film_weights(name="c5", n_train=1000, n_val=2000, seed_train=11, seed_va
     if best is None:  # nothing beat the fallback-free bar: keep the physics start
         best = "neumann"
     report["selected"] = best
+    # the graph size: more neighbours cost little next to the coupling operator
+    best_k, best_kit = k, best_it
+    for kk in (24, 32, 48):
+        info, rel = solve_iterations(val, cands[best], k=kk)
+        report["val_k%d" % kk] = info
+        ok = info["converged"] == 16 and float(rel.max()) <= 1e-6 and info["precond_fallbacks"] == 0
+        log("%s at k=%d: %d iterations, %.3f s, ok %s" % (best, kk, info["iterations"], info["device_seconds"], ok))
+        if ok and best_kit is not None and info["iterations"] < best_kit:
+            best_k, best_kit = kk, info["iterations"]
+    report["k"] = best_k
     return cands[best], report
 
 
@@ -379,7 +389,8 @@ def main(argv=None):
     a = ap.parse_args(argv)
     p, rep = fit_film_weights(a.shape, a.n_train, a.n_val)
     name = a.out or "precond_%s" % a.shape
-    path = save_params(p, name, meta={"report": json.dumps(rep, default=float)}, directory=a.dir)
+    path = save_params(p, name, meta={"report": json.dumps(rep, default=float), "k": np.int32(rep["k"])},
+                       directory=a.dir)
     print(json.dumps(rep, default=float))
     print("wrote", path)
 

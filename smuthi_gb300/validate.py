@@ -74,7 +74,7 @@ def main(argv=None):
     if a.precond != "none":
         cand = "precond_%s" % a.workload if a.precond == "auto" else a.precond
         if os.path.exists(os.path.join(learned.DATA_DIR, cand + ".npz")):
-            learned.use(system, learned.load_params(cand, bs))
+            learned.use(system, learned.load_params(cand, bs), k=learned.load_meta(cand)["k"])
             prec, pname = base | _lib.SG_PRECOND, cand
     out = {"workload": a.workload, "n_spheres": system["n"], "nrhs": a.nrhs, "preconditioner": pname}
     # one FP32 operator application first: it runs the FP32 kernel autotuner, which times its

@@ -226,8 +226,9 @@ def test_committed_weights_reduce_iterations_on_held_out_film(gpu_context):
     from smuthi_gb300 import learned
     val = learned.film_system("c5", 1000, nrhs=16, seed=31, ctx=gpu_context)
     weights = learned.load_params("precond_c5", val["blocksize"])
+    k = learned.load_meta("precond_c5")["k"]
     base, rel0 = learned.solve_iterations(val)
-    info, rel = learned.solve_iterations(val, weights)
+    info, rel = learned.solve_iterations(val, weights, k=k)
     assert rel0.max() <= 1e-6 and rel.max() <= 1e-6
     assert info["converged"] == 16 and info["precond_fallbacks"] == 0
     assert info["iterations"] < base["iterations"]
