@@ -288,3 +288,28 @@ def test_tensor_core_operator_matches_fp64(name, gpu_context):
             ref = fn(X, _lib.SG_FP64)
             tc = fn(X, _lib.SG_TF32X3)
             assert gc.relerr(tc, ref) < 1e-5, (R, fn.__name__, gc.relerr(tc, ref))
+
+
+@pytest.mark.parametrize("count", [1, 2])
+def test_one_and_two_particle_systems(count, gpu_context):
+    """Smallest systems (the self pair only, one pair): every precision against the oracle's FP64
+    operator, and the plain and chosen solves to their tolerances."""
+    from smuthi_gb300 import _lib
+    g = gc.load("c5s")
+    sub = {k: g[k] for k in g}
+    for key in ("positions", "n_particle", "radii", "l_max", "m_max"):
+        sub[key] = g[key][:count]
+    parts, ls, wl, W, M = _product_system(sub, "linear", gpu_context)
+    oparts, _, _ = gc.oracle_inputs(sub)
+    Wo = osv.RadialLookupCPU(oparts, W.lookup_table, W.radial_distance_array, "linear")
+    rng = np.random.default_rng(count)
+    x = rng.standard_normal(W.shape[0]) + 1j * rng.standard_normal(W.shape[0])
+    ref = Wo.matvec(x)
+    assert gc.relerr(W.linear_operator.matvec(x), ref) < 1e-12
+    assert gc.relerr(gpu_context.coupling_matvec(x, _lib.SG_DF64), ref) < 1e-12
+    assert gc.relerr(gpu_context.coupling_matvec(x, _lib.SG_FP32), ref) < 1e-5
+    b = np.ascontiguousarray(x)
+    for prec, tol in ((_lib.SG_FP64, 1e-12), (_lib.SG_FP32 | _lib.SG_DF64, 1e-6)):
+        sol, info = gpu_context.gmres(b, np.zeros_like(b), tol, precision=prec)
+        assert info.converged == 1
+        assert gpu_context.true_residual(b, sol)[0] <= tol
