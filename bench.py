@@ -98,7 +98,9 @@ def algorithmic_bytes(n, bs, kind, n_int, nrhs, fp32):
 # ----------------------------------------------------------------------------------------- clocks
 class ClockSampler:
     def __init__(self, device):
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+        import tempfile
+        self.path = os.path.join(os.environ.get("SG_CLOCK_LOG_DIR", tempfile.gettempdir()),
+                                 "clocks_bench_%d.csv" % os.getpid())
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"

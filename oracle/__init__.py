@@ -9,7 +9,7 @@ operator, scipy GMRES and the extinction / total scattering cross sections.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
 leg (and its ``--impl reference`` arm) may import it, and only as the
-checker or as the timed CPU baseline. The product package ``smuthi_gb300``
+values a test compares against or as the timed CPU baseline. The product package ``smuthi_gb300``
 never imports it and has no CPU fallback.
 
 Parity pin: the oracle is checked against (a) golden vectors generated by
