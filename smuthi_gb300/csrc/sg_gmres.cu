@@ -944,11 +944,8 @@ static GmresResult refine_mixed(Solver &S, const double2 *b, double2 *x, double 
     }
     prev_worst = worst;
     // correction solve with the FP32 operator: tolerance relative to the current residual
-    // (floor 5e-7: the first correction of a 1e-6 solve then ends below the tolerance with margin, so
-    // the FP64-grade residual after it rarely lands just above 1e-6 and forces a second step; still
-    // well above the FP32 operator's noise floor of ~1e-7)
     double tau = 0.3 * rtol / worst;
-    tau = std::max(5e-7, std::min(0.5, tau));
+    tau = std::max(1e-6, std::min(0.5, tau));
     k_zero(d, len, S.st);
     const int cycles = std::max(1, std::min(inner_cap_cycles, (maxiter - inner_total) / restart + 1));
     GmresResult g;
