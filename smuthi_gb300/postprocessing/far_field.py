@@ -109,6 +109,14 @@ def scattered_pwe(vacuum_wavelength, layer_system, xy, z, l_max, m_max, coefs, l
     return out_up, out_dn
 
 
+def _simulation_context(simulation, context):
+    """The GPU context of a simulation's coupling matrix, when the caller gave none."""
+    if context is not None or simulation is None:
+        return context
+    cm = getattr(getattr(simulation, 'linear_system', None), 'coupling_matrix', None)
+    return getattr(cm, 'context', None)
+
+
 def _incidence(initial_field, layer_system):
     i_top = layer_system.number_of_layers() - 1
     i_P = 0 if np.cos(initial_field.polar_angle) > 0 else i_top
@@ -122,6 +130,7 @@ def extinction_cross_section(simulation=None, initial_field=None, particle_list=
                              coefficients=None, context=None):
     """Extinction cross section (top plus bottom extinction) of a plane wave (``context``: GPU particle
     sum, see ``scattered_pwe``)."""
+    context = _simulation_context(simulation, context)
     initial_field = initial_field or simulation.initial_field
     particle_list = particle_list or simulation.particle_list
     layer_system = layer_system or simulation.layer_system
@@ -158,6 +167,7 @@ def total_scattering_cross_section(simulation=None, initial_field=None, particle
                                    coefficients=None, context=None):
     """Angle-integrated scattering cross section (trapezoidal rule over the far-field grid;
     ``context``: GPU particle sum, see ``scattered_pwe``)."""
+    context = _simulation_context(simulation, context)
     initial_field = initial_field or simulation.initial_field
     particle_list = particle_list or simulation.particle_list
     layer_system = layer_system or simulation.layer_system

@@ -181,6 +181,11 @@ def test_simulation_api_end_to_end(gpu_context):
     np.testing.assert_array_equal(flds.default_Sommerfeld_k_parallel_array, g["kpar"])
     b = np.concatenate([p.scattered_field.coefficients for p in parts])
     assert gc.relerr(b, g["b_linear_w0"]) < 1e-10
+    # cross sections through the simulation: the particle sums run on the simulation's GPU context
+    from smuthi_gb300.postprocessing import far_field as ff
+    assert abs(ff.extinction_cross_section(sim) - g["sigma_ext_linear_w0"]) <= 1e-9 * abs(g["sigma_ext_linear_w0"])
+    assert abs(ff.total_scattering_cross_section(sim) - g["sigma_sca_linear_w0"]) <= 1e-9 * abs(
+        g["sigma_sca_linear_w0"])
 
 
 def test_full_size_c2_properties(gpu_context):
