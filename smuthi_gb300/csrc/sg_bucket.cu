@@ -333,11 +333,9 @@ static void launch_bucket_t(const BucketArgs &a, cudaStream_t st) {
   const size_t smem = ((size_t)NC * a.bs * a.bs + (size_t)a.T * a.bs * RT + (size_t)(kBThreads / 32) * a.bs * RT) *
                       sizeof(float2);
   SG_REQUIRE(smem <= 220 * 1024, "bucketed operator: shared memory request too large");
-  static bool attr = false;
-  if (!attr) {
+  static bool attr[64] = {};
+  if (first_on_device(attr))
     SG_CUDA(cudaFuncSetAttribute(bucket_kernel<NC, RT, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-    attr = true;
-  }
   dim3 grid(a.T > 0 ? (unsigned)((size_t)((a.n + a.T - 1) / a.T) * a.S) : 0u, a.R / RT);
   bucket_kernel<NC, RT, P><<<grid, kBThreads, smem, st>>>(a);
   SG_CUDA(cudaGetLastError());

@@ -347,12 +347,10 @@ static void launch_t(const CouplingLaunch &L, int nsplit, cudaStream_t st) {
   const int nw = kThreads / 32;
   const size_t smem = (size_t)nw * L.bs * RT * sizeof(cplx) + (size_t)L.bs * RT * sizeof(double2);
   // the cross-warp reduction reuses the u buffers; they must hold nw*bs*RT partials
-  static bool attr_done = false;
-  if (!attr_done) {
+  static bool attr_done[64] = {};
+  if (first_on_device(attr_done))
     SG_CUDA(cudaFuncSetAttribute(coupling_kernel<Real, NC, RT, P, PAIRS>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr_done = true;
-  }
   dim3 grid(L.n, nsplit, L.nrhs / RT);
   coupling_kernel<Real, NC, RT, P, PAIRS><<<grid, kThreads, smem, st>>>(L, nsplit);
   SG_CUDA(cudaGetLastError());

@@ -121,6 +121,16 @@ void k_scatter(const double2 *src, double2 *dst, const int *map, int n_unknowns,
 void k_zero(double2 *p, size_t n, cudaStream_t st);
 void k_to_f32(const double2 *x, float2 *y, size_t n, cudaStream_t st);
 
+// cudaFuncSetAttribute acts on the current device: true the first time a given kernel's attribute is
+// needed on the current device (the caller keeps one flag array per kernel instantiation)
+inline bool first_on_device(bool (&done)[64]) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return true;
+  if (done[dev]) return false;
+  done[dev] = true;
+  return true;
+}
+
 // FMA-throughput probe (TFLOP/s) of the FP64 or FP32 pipe
 double fma_peak(int fp64, cudaStream_t st);
 

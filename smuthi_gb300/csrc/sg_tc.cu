@@ -345,11 +345,9 @@ static void tc_launch_t(const TcArgs &a, cudaStream_t st) {
   constexpr int NN = 2 * R;
   const size_t smem = (size_t)(4 * 128 * kBP + 4 * NN * kBP) * sizeof(float) + 2 * 2 * 33 * sizeof(float2) +
                       4 * sizeof(int) + 6 * sizeof(float) + 2 * sizeof(uint64_t) + 2 * sizeof(uint32_t) + 64;
-  static bool attr_done = false;
-  if (!attr_done) {
+  static bool attr_done[64] = {};
+  if (first_on_device(attr_done))
     SG_CUDA(cudaFuncSetAttribute(tc_coupling_kernel<NC, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_done = true;
-  }
   tc_coupling_kernel<NC, R><<<(a.n + 1) / 2, kTcThreads, smem, st>>>(a);
   SG_CUDA(cudaGetLastError());
 }
