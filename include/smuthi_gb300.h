@@ -90,6 +90,23 @@ int sg_set_particles(sg_context *ctx, int n_particles, const double *xy, int n_u
 int sg_set_lookup(sg_context *ctx, int kind, int len_rho, double rho_min, double resolution,
                   const double *table);
 
+/* Volume lookup for particles at different heights in one layer, replacing the radial table
+ * (the table upload and kernel compile of CouplingMatrixVolumeLookupCUDA,
+ * smuthi/linearsystem/linear_system.py:700-770, and the interpolators of
+ * CouplingMatrixVolumeLookupCPU, :592-667). z[i]: height of particle i (the xy of sg_set_particles).
+ * table_plus[rho][s][n1][n2] is the z1 + z2 table on rho_min + a * resolution, sz_min + s * resolution;
+ * table_minus[rho][d][n1][n2] the z1 - z2 table (direct + layer-mediated) on dz_min + d * resolution
+ * (complex, len_rho x len_z x blocksize^2 each; the layout and grids of
+ * smuthi/linearsystem/particlecoupling/prepare_lookup.py:16-250). kind: SG_LINEAR (bilinear),
+ * SG_CUBIC (tensor-product not-a-knot cubic spline = RectBivariateSpline(kx=ky=3) of the CPU class)
+ * or SG_CUBIC_HERMITE (the 4 x 4-tap Catmull-Rom of the reference CUDA kernel). The grids must
+ * cover every pair's (rho, z_i + z_j, z_i - z_j) with all interpolation taps. With a volume lookup
+ * the operator supports SG_FP64 and SG_FP32 (solves: SG_FP64, SG_FP32 [| SG_BLOCK_GMRES]); a later
+ * sg_set_lookup or sg_set_particles drops it. */
+int sg_set_volume_lookup(sg_context *ctx, int kind, const double *z, int len_rho, double rho_min, int len_z,
+                         double sz_min, double dz_min, double resolution, const double *table_plus,
+                         const double *table_minus);
+
 /* Per-particle T-matrices (smuthi/linearsystem/linear_system.py:410-424):
  * n_types distinct blocks t[type][n1][n2] in the global lookup index space
  * (blocksize x blocksize complex); particle_type[i] picks particle i's block.
@@ -200,6 +217,13 @@ int sg_bessel_jac_table(sg_context *ctx, const void *kappa, const void *jac, int
 int sg_farfield_sum(sg_context *ctx, int n_particles, const void *xy, int blocksize, int nrhs, const void *coef,
                     int m_max, const int32_t *m_of_n, int nk, const void *kpar, const void *S, int na,
                     const void *alpha, void *out, void *stream);
+
+/* The same for particles at different heights: zphase complex128[nk][n_particles] (device) multiplies
+ * particle i's term at kpar_k (exp(+-i k_z (z_ref - z_i)) of the up- or downgoing expansion; the
+ * reference applies it per particle in smuthi/fields/transformations.py:133-233). NULL = no factor. */
+int sg_farfield_sum_heights(sg_context *ctx, int n_particles, const void *xy, int blocksize, int nrhs,
+                            const void *coef, int m_max, const int32_t *m_of_n, int nk, const void *kpar,
+                            const void *S, int na, const void *alpha, const void *zphase, void *out, void *stream);
 
 /* ---------------------------------------------------------------------------------------------
  * Learned preconditioner for the mixed solve (no counterpart in the reference, whose GMRES call

@@ -31,7 +31,7 @@ EXPORTS = ("sg_last_error", "sg_version", "sg_create", "sg_destroy", "sg_set_par
            "sg_coupling_matvec_linear_noalloc", "sg_precond_param_count", "sg_precond_add_graph",
            "sg_precond_select", "sg_precond_clear", "sg_precond_set_params", "sg_precond_get_params",
            "sg_precond_apply_dev", "sg_precond_train_step", "sg_precond_export_blocks", "sg_bessel_jac_table",
-           "sg_farfield_sum")
+           "sg_farfield_sum", "sg_set_volume_lookup", "sg_farfield_sum_heights")
 
 
 class LibraryMissing(RuntimeError):
@@ -73,6 +73,7 @@ def _declare(L):
         "sg_destroy": [_P],
         "sg_set_particles": [_P, _I, _P, _I, _P, _P, _I, _P],
         "sg_set_lookup": [_P, _I, _I, _D, _D, _P],
+        "sg_set_volume_lookup": [_P, _I, _P, _I, _D, _I, _D, _D, _D, _P, _P],
         "sg_set_tmatrix": [_P, _I, _P, _P, _I],
         "sg_coupling_matvec": [_P, _P, _P, _I, _I],
         "sg_master_matvec": [_P, _P, _P, _I, _I],
@@ -89,6 +90,7 @@ def _declare(L):
         "sg_coupling_matvec_linear_noalloc": [_I, _I, _P, _I, _P, _I, _D, _D, _P, _P, _P, _I, _P],
         "sg_bessel_jac_table": [_P, _P, _P, _I, _P, _I, _I, _P, _P],
         "sg_farfield_sum": [_P, _I, _P, _I, _I, _P, _I, _P, _I, _P, _P, _I, _P, _P, _P],
+        "sg_farfield_sum_heights": [_P, _I, _P, _I, _I, _P, _I, _P, _I, _P, _P, _I, _P, _P, _P, _P],
         "sg_precond_param_count": [_I],
         "sg_precond_add_graph": [_P, _I, _P, ctypes.POINTER(_I)],
         "sg_precond_select": [_P, _I],
@@ -166,6 +168,17 @@ class Context:
         tab = np.ascontiguousarray(table, dtype=np.complex128)
         check(lib().sg_set_lookup(self.h, KINDS[kind] if isinstance(kind, str) else int(kind), tab.shape[0],
                                   float(rho_min), float(resolution), ptr(tab)))
+
+    def set_volume_lookup(self, kind, z, table_plus, table_minus, rho_min, sz_min, dz_min, resolution):
+        """Volume lookup [rho, z, n1, n2] tables (z1 + z2 and z1 - z2) and the particle heights."""
+        zz = np.ascontiguousarray(z, dtype=np.float64)
+        tp = np.ascontiguousarray(table_plus, dtype=np.complex128)
+        tm = np.ascontiguousarray(table_minus, dtype=np.complex128)
+        if tp.shape != tm.shape or tp.ndim != 4:
+            raise ValueError("volume tables must both be [len_rho, len_z, blocksize, blocksize]")
+        check(lib().sg_set_volume_lookup(self.h, KINDS[kind] if isinstance(kind, str) else int(kind), ptr(zz),
+                                         tp.shape[0], float(rho_min), tp.shape[1], float(sz_min), float(dz_min),
+                                         float(resolution), ptr(tp), ptr(tm)))
 
     def set_tmatrix(self, blocks, particle_type, diagonal):
         t = np.ascontiguousarray(blocks, dtype=np.complex128)
@@ -295,12 +308,15 @@ class Context:
                                         ctypes.c_void_p(stream or 0)))
 
     def farfield_sum_dev(self, n, xy_ptr, bs, nrhs, coef_ptr, m_max, m_of_n, nk, kpar_ptr, S_ptr, na, alpha_ptr,
-                         out_ptr, stream=None):
+                         out_ptr, stream=None, zphase_ptr=None):
+        """Device particle sum of the scattered plane-wave expansion (``zphase_ptr``: per-particle
+        height factors [nk][n] for particles at different heights, None when they share one)."""
         mo = np.ascontiguousarray(m_of_n, dtype=np.int32)
-        check(lib().sg_farfield_sum(self.h, int(n), ctypes.c_void_p(xy_ptr), int(bs), int(nrhs),
-                                    ctypes.c_void_p(coef_ptr), int(m_max), ptr(mo), int(nk), ctypes.c_void_p(kpar_ptr),
-                                    ctypes.c_void_p(S_ptr), int(na), ctypes.c_void_p(alpha_ptr),
-                                    ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream or 0)))
+        check(lib().sg_farfield_sum_heights(self.h, int(n), ctypes.c_void_p(xy_ptr), int(bs), int(nrhs),
+                                            ctypes.c_void_p(coef_ptr), int(m_max), ptr(mo), int(nk),
+                                            ctypes.c_void_p(kpar_ptr), ctypes.c_void_p(S_ptr), int(na),
+                                            ctypes.c_void_p(alpha_ptr), ctypes.c_void_p(zphase_ptr or 0),
+                                            ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream or 0)))
 
     def launch_count(self):
         n = ctypes.c_int64()

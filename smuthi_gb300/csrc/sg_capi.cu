@@ -45,7 +45,7 @@ static void require_ready(sg_context *c, bool need_t) {
 // FP32 operator data: the pair table of the per-receiver kernel and, when the sizes allow it, the
 // interval-bucketed plan; the autotuner picks between the two kernels per RHS count.
 static void ensure_pairs(sg_context *c, cudaStream_t st) {
-  if (c->pairs_ready) return;
+  if (c->pairs_ready || c->vol) return;  // the volume kernel needs no pair table
   c->pairs.reserve((size_t)c->n * c->n);
   sg::build_pairs(c->pos.ptr, c->n, c->rho_min, c->res, c->n_int, c->pairs.ptr, st);
   c->launches += 1;
@@ -157,6 +157,7 @@ int sg_set_particles(sg_context *ctx, int n_particles, const double *xy, int n_u
     ctx->pairs_ready = false;
     ctx->tuned_df.clear();
     ctx->kind = -1;  // the table must be re-uploaded for a new geometry
+    ctx->vol = false;
     ctx->t_ready = false;
     ctx->pgraphs.clear();  // preconditioner graphs belong to the old particles
     ctx->p_active = -1;
@@ -201,6 +202,7 @@ int sg_set_lookup(sg_context *ctx, int kind, int len_rho, double rho_min, double
     sg::build_coefficients(kind, raw.ptr, len_rho, bs, ctx->coef64.ptr, ctx->coef32.ptr, work.ptr, st);
     ctx->launches += kind == SG_CUBIC ? 2 : 1;
     ctx->kind = kind;
+    ctx->vol = false;
     ctx->len_rho = len_rho;
     ctx->n_int = n_int;
     ctx->ncoef = ncoef;
@@ -210,6 +212,82 @@ int sg_set_lookup(sg_context *ctx, int kind, int len_rho, double rho_min, double
     ctx->df_ready = false;
     ctx->tuned_df.clear();
     ctx->pgraphs.clear();  // their near-field blocks came from the old table
+    ctx->p_active = -1;
+    return SG_OK;
+  });
+}
+
+int sg_set_volume_lookup(sg_context *ctx, int kind, const double *z, int len_rho, double rho_min, int len_z,
+                         double sz_min, double dz_min, double resolution, const double *table_plus,
+                         const double *table_minus) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx != nullptr, "null context");
+    SG_REQUIRE(ctx->n > 0, "sg_set_particles must precede sg_set_volume_lookup");
+    SG_REQUIRE(kind == SG_LINEAR || kind == SG_CUBIC || kind == SG_CUBIC_HERMITE, "unknown interpolation kind");
+    const int need_len = kind == SG_LINEAR ? 2 : 4;
+    SG_REQUIRE(len_rho >= need_len && len_z >= need_len, "lookup grid too short for this interpolation kind");
+    SG_REQUIRE(resolution > 0 && std::isfinite(resolution) && std::isfinite(rho_min) && std::isfinite(sz_min) &&
+                   std::isfinite(dz_min),
+               "bad lookup grid");
+    SG_REQUIRE(z && table_plus && table_minus, "null input array");
+    const int bs = ctx->bs, N = ctx->n;
+    SG_REQUIRE(all_finite(z, N), "particle heights must be finite");
+    const size_t count = (size_t)len_rho * len_z * bs * bs;
+    if (!all_finite(table_plus, 2 * count) || !all_finite(table_minus, 2 * count))
+      throw sg::Error{SG_ERR_NAN, "lookup table holds NaN or Inf"};
+    // every pair's (rho, z_i + z_j, z_i - z_j) must lie where all taps are on the grid
+    std::vector<double2> pos(N);
+    use_device(ctx);
+    SG_CUDA(cudaMemcpy(pos.data(), ctx->pos.ptr, N * sizeof(double2), cudaMemcpyDeviceToHost));
+    double r2max = 0.0, zmin = z[0], zmax = z[0];
+    for (int i = 0; i < N; ++i) {
+      zmin = std::min(zmin, z[i]);
+      zmax = std::max(zmax, z[i]);
+      for (int j = i + 1; j < N; ++j) {
+        const double dx = pos[i].x - pos[j].x, dy = pos[i].y - pos[j].y;
+        r2max = std::max(r2max, dx * dx + dy * dy);
+      }
+    }
+    const int lo = kind == SG_CUBIC_HERMITE ? 1 : 0, hi = kind == SG_CUBIC_HERMITE ? 3 : 2;
+    auto covers = [&](double origin, double a, double b, int len) {
+      return std::floor((a - origin) / resolution) >= lo && std::floor((b - origin) / resolution) + hi <= len;
+    };
+    SG_REQUIRE(covers(rho_min, 0.0, std::sqrt(r2max), len_rho),
+               "lookup grid does not cover [0, largest lateral particle distance]");
+    SG_REQUIRE(covers(sz_min, 2 * zmin, 2 * zmax, len_z), "z1 + z2 grid does not cover the particle heights");
+    SG_REQUIRE(covers(dz_min, zmin - zmax, zmax - zmin, len_z), "z1 - z2 grid does not cover the particle heights");
+    cudaStream_t st = ctx->stream;
+    const int nq = kind == SG_CUBIC ? 4 : 1;
+    sg::DevBuf<double2> raw;
+    raw.reserve(count);
+    ctx->vpl64.reserve(count * nq);
+    ctx->vmn64.reserve(count * nq);
+    ctx->vpl32.reserve(count * nq);
+    ctx->vmn32.reserve(count * nq);
+    SG_CUDA(cudaMemcpyAsync(raw.ptr, table_plus, count * sizeof(double2), cudaMemcpyHostToDevice, st));
+    sg::build_volume_table(kind, raw.ptr, len_rho, len_z, bs, ctx->vpl64.ptr, ctx->vpl32.ptr, st);
+    SG_CUDA(cudaMemcpyAsync(raw.ptr, table_minus, count * sizeof(double2), cudaMemcpyHostToDevice, st));
+    sg::build_volume_table(kind, raw.ptr, len_rho, len_z, bs, ctx->vmn64.ptr, ctx->vmn32.ptr, st);
+    ctx->launches += 2 * (kind == SG_CUBIC ? 4 : 1);
+    ctx->vz.reserve(N);
+    SG_CUDA(cudaMemcpy(ctx->vz.ptr, z, N * sizeof(double), cudaMemcpyHostToDevice));
+    ctx->kind = kind;
+    ctx->vol = true;
+    ctx->len_rho = len_rho;
+    ctx->rho_min = rho_min;
+    ctx->res = resolution;
+    ctx->v_len_z = len_z;
+    ctx->v_nq = nq;
+    ctx->v_sz_min = sz_min;
+    ctx->v_dz_min = dz_min;
+    ctx->n_int = 0;
+    ctx->ncoef = 0;
+    ctx->pairs_ready = false;
+    ctx->use_bucket = false;
+    ctx->tuned.clear();
+    ctx->df_ready = false;
+    ctx->tuned_df.clear();
+    ctx->pgraphs.clear();
     ctx->p_active = -1;
     return SG_OK;
   });
@@ -271,6 +349,8 @@ static void matvec_dev(sg_context *c, const double2 *x, double2 *y, int R, int p
   SG_REQUIRE(R >= 1 && R <= 256, "nrhs must be in [1, 256]");
   SG_REQUIRE(precision == SG_FP64 || precision == SG_FP32 || precision == SG_DF64 || precision == SG_TF32X3,
              "unknown precision");
+  SG_REQUIRE(!c->vol || precision == SG_FP64 || precision == SG_FP32,
+             "a volume lookup supports SG_FP64 and SG_FP32 only");
   use_device(c);
   const bool fp32 = precision == SG_FP32;
   if (fp32 || precision == SG_TF32X3) ensure_pairs(c, st);
@@ -361,6 +441,8 @@ static int solve_dev_impl(sg_context *ctx, const double2 *b, double2 *x, int nrh
                  ((precision & SG_FP32) && !(precision & ~(SG_FP32 | SG_BLOCK_GMRES | SG_PRECOND | SG_DF64)) &&
                   !((precision & SG_BLOCK_GMRES) && (precision & SG_PRECOND))),
              "unknown precision / solver flags");
+  SG_REQUIRE(!ctx->vol || !(precision & (SG_PRECOND | SG_DF64)),
+             "a volume lookup supports SG_FP64 and SG_FP32 (| SG_BLOCK_GMRES) solves only");
   if (precision & SG_PRECOND) {
     SG_REQUIRE(ctx->p_active >= 0, "SG_PRECOND needs a preconditioner graph (sg_precond_select)");
     SG_REQUIRE(ctx->p_count == sg::precond_param_count(ctx->bs), "SG_PRECOND needs parameters (sg_precond_set_params)");
@@ -533,18 +615,26 @@ int sg_bessel_jac_table(sg_context *ctx, const void *kappa, const void *jac, int
   });
 }
 
-int sg_farfield_sum(sg_context *ctx, int n_particles, const void *xy, int blocksize, int nrhs, const void *coef,
-                    int m_max, const int32_t *m_of_n, int nk, const void *kpar, const void *S, int na,
-                    const void *alpha, void *out, void *stream) {
+int sg_farfield_sum_heights(sg_context *ctx, int n_particles, const void *xy, int blocksize, int nrhs,
+                            const void *coef, int m_max, const int32_t *m_of_n, int nk, const void *kpar,
+                            const void *S, int na, const void *alpha, const void *zphase, void *out, void *stream) {
   return guarded([&]() -> int {
     SG_REQUIRE(ctx && xy && coef && m_of_n && kpar && S && alpha && out, "null argument");
     use_device(ctx);
     cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
     sg::farfield_sum((const double2 *)xy, n_particles, blocksize, nrhs, (const double2 *)coef, m_max, m_of_n, nk,
-                     (const double *)kpar, (const double2 *)S, na, (const double *)alpha, (double2 *)out, st);
+                     (const double *)kpar, (const double2 *)S, na, (const double *)alpha, (const double2 *)zphase,
+                     (double2 *)out, st);
     ctx->launches += 1;
     return SG_OK;
   });
+}
+
+int sg_farfield_sum(sg_context *ctx, int n_particles, const void *xy, int blocksize, int nrhs, const void *coef,
+                    int m_max, const int32_t *m_of_n, int nk, const void *kpar, const void *S, int na,
+                    const void *alpha, void *out, void *stream) {
+  return sg_farfield_sum_heights(ctx, n_particles, xy, blocksize, nrhs, coef, m_max, m_of_n, nk, kpar, S, na, alpha,
+                                 nullptr, out, stream);
 }
 
 int sg_precond_param_count(int blocksize) {

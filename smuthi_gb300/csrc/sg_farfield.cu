@@ -9,7 +9,9 @@
 //
 // (S: the SVWF -> plane-wave transformation coefficient of multipole n and polarisation p at
 // kappa_k, computed on the host; the k-dependent prefactor and the layer response are applied on
-// the host afterwards). On the host this is a dense N-long contraction for every (k, a, r, p):
+// the host afterwards). Particles at different heights carry a per-particle factor
+// zphase[k][i] = exp(+-i k_z,k (z_ref - z_i)) inside the sum (null: all at one height, the factor is
+// part of the host prefactor). On the host this is a dense N-long contraction for every (k, a, r, p):
 // 72 s for 1000 particles and one RHS on the default angular grid, so hours at 10 000 particles and
 // 16 RHS. Here one thread owns one azimuth a of one kappa_k and a tile of CT (r, p) columns; a block
 // stages, for a chunk of CH particles, the m-resolved data D[m][i][col] = sum_{n: m(n) = m}
@@ -35,6 +37,7 @@ struct FfArgs {
   const double *alpha;   // [A]
   const int *moff;       // [nm + 1] CSR over m = -mmax..mmax of the n with that m
   const int *mlist;      // [B]
+  const double2 *zph;    // [K][N] per-particle height factor, or null
   double2 *out;          // [R][2][K][A]
   int N, B, R, K, A, mmax;
 };
@@ -78,6 +81,10 @@ __global__ void __launch_bounds__(kFfThreads) ff_sum_kernel(const FfArgs f) {
           v.x = fma(cv.x, sv.x, fma(-cv.y, sv.y, v.x));
           v.y = fma(cv.x, sv.y, fma(cv.y, sv.x, v.y));
         }
+        if (f.zph) {
+          const double2 zp = f.zph[(size_t)k * f.N + i];
+          v = make_double2(v.x * zp.x - v.y * zp.y, v.x * zp.y + v.y * zp.x);
+        }
       }
       D[e] = v;
     }
@@ -114,8 +121,8 @@ __global__ void __launch_bounds__(kFfThreads) ff_sum_kernel(const FfArgs f) {
 }
 
 void farfield_sum(const double2 *xy, int n, int bs, int nrhs, const double2 *coef, int mmax, const int *mofn_host,
-                  int nk, const double *kpar, const double2 *S, int na, const double *alpha, double2 *out,
-                  cudaStream_t st) {
+                  int nk, const double *kpar, const double2 *S, int na, const double *alpha, const double2 *zphase,
+                  double2 *out, cudaStream_t st) {
   SG_REQUIRE(n >= 1 && bs >= 1 && nrhs >= 1 && nk >= 1 && na >= 1, "empty far-field problem");
   SG_REQUIRE(mmax >= 0 && mmax <= kFfMaxM, "m_max must be in [0, 16]");
   const int nm = 2 * mmax + 1;
@@ -132,7 +139,7 @@ void farfield_sum(const double2 *xy, int n, int bs, int nrhs, const double2 *coe
   d_mlist.reserve(bs);
   SG_CUDA(cudaMemcpyAsync(d_moff.ptr, moff.data(), (nm + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
   SG_CUDA(cudaMemcpyAsync(d_mlist.ptr, mlist.data(), bs * sizeof(int), cudaMemcpyHostToDevice, st));
-  FfArgs f{xy, coef, S, kpar, alpha, d_moff.ptr, d_mlist.ptr, out, n, bs, nrhs, nk, na, mmax};
+  FfArgs f{xy, coef, S, kpar, alpha, d_moff.ptr, d_mlist.ptr, zphase, out, n, bs, nrhs, nk, na, mmax};
   const size_t smem = (size_t)nm * kFfCH * kFfCT * sizeof(double2);
   SG_CUDA(cudaFuncSetAttribute(ff_sum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid(nk, (na + kFfThreads - 1) / kFfThreads, (2 * nrhs + kFfCT - 1) / kFfCT);

@@ -1120,7 +1120,10 @@ void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool maste
     SG_CUDA(cudaEventRecord(e0, st));
   }
   int variant = 0, rt = 0;
-  if (fp32) {
+  if (c->vol) {
+    c->launches += launch_volume(c, x, y, R, master, fp32, st);
+    variant = -1;
+  } else if (fp32) {
     variant = -1;
     for (const auto &t : c->tuned)
       if (t.nrhs == R) {
@@ -1134,7 +1137,7 @@ void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool maste
   }
   if (variant == 1) {
     c->launches += launch_bucket_matvec(c, x, y, R, master, st);
-  } else {
+  } else if (variant == 0) {
     CouplingLaunch L{};
     L.pos = c->pos.ptr;
     L.mofn = c->mofn.ptr;

@@ -134,14 +134,21 @@ inline bool first_on_device(bool (&done)[64]) {
 // FMA-throughput probe (TFLOP/s) of the FP64 or FP32 pipe
 double fma_peak(int fp64, cudaStream_t st);
 
+// volume lookup (sg_volume.cu): raw [len_rho][len_z][bs][bs] (n2 fastest) -> interpolation planes
+// [len_rho][len_z][nq][bs][bs] (n1 fastest; nq = 4 for SG_CUBIC, else 1) in FP64 and FP32
+void build_volume_table(int kind, const double2 *raw, int len_rho, int len_z, int bs, double2 *out64, float2 *out32,
+                        cudaStream_t st);
+// y = W x or x - T W x with the volume lookup on padded vectors; returns the number of kernels launched
+int launch_volume(sg_context *c, const double2 *x, double2 *y, int R, bool master, bool fp32, cudaStream_t st);
+
 // Bessel factors of the layer-mediated lookup table (sg_table.cu)
 void bessel_jac_table(const double2 *kp, const double2 *jac, int nk, const double *rho, int nr, int nmax,
                       double2 *out, cudaStream_t st);
 
 // particle sum of the scattered plane-wave expansion (sg_farfield.cu); synchronous
 void farfield_sum(const double2 *xy, int n, int bs, int nrhs, const double2 *coef, int mmax, const int *mofn_host,
-                  int nk, const double *kpar, const double2 *S, int na, const double *alpha, double2 *out,
-                  cudaStream_t st);
+                  int nk, const double *kpar, const double2 *S, int na, const double *alpha, const double2 *zphase,
+                  double2 *out, cudaStream_t st);
 
 // ---------------------------------------------------------------- learned preconditioner (sg_precond.cu)
 int precond_param_count(int bs);
@@ -183,6 +190,15 @@ struct sg_context {
   sg::DevBuf<int> tc_err;    // tensor-core operator: set when a bounded wait ran out
   bool tc_err_init = false;
   bool pairs_ready = false;  // FP32 operator data (bucket plan or pair table) is built
+
+  // volume lookup (particles at different heights): replaces the radial table when set; `kind`,
+  // `len_rho`, `rho_min` and `res` describe its rho axis
+  bool vol = false;
+  int v_len_z = 0, v_nq = 1;
+  double v_sz_min = 0, v_dz_min = 0;
+  sg::DevBuf<double> vz;                // [N] particle heights
+  sg::DevBuf<double2> vpl64, vmn64;     // z1 + z2 and z1 - z2 tables, [rho][z][q][n2][n1]
+  sg::DevBuf<float2> vpl32, vmn32;
 
   // interval-bucketed FP32 operator (sg_bucket.cu)
   bool use_bucket = false;  // the bucket plan exists

@@ -438,6 +438,7 @@ __global__ void pc_adam_kernel(float *w, const float *g, float *m, float *v, siz
 void precond_add_graph(sg_context *c, int k, const int *nbr_host, int *graph_id, cudaStream_t st) {
   SG_REQUIRE(c->t_ready && c->t_diag, "the learned preconditioner needs diagonal T-matrices (sg_set_tmatrix)");
   SG_REQUIRE(c->kind >= 0, "sg_set_lookup must precede the preconditioner graph");
+  SG_REQUIRE(!c->vol, "the learned preconditioner needs a radial lookup (particles at one height)");
   SG_REQUIRE(k >= 0 && k <= 64, "k must be in [0, 64]");
   SG_REQUIRE(c->bs <= 64, "the learned preconditioner supports blocksize <= 64");
   SG_REQUIRE(c->uniform, "the learned preconditioner works on uniform particle blocks");

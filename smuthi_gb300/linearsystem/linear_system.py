@@ -8,9 +8,13 @@ the same name (:813-900): same constructor, a ``SystemMatrix`` with
 lookup, and ``LinearSystem.solve`` runs GMRES on the device through the C ABI
 (``sg_gmres_solve``) with the reference's call semantics (:271-286).
 
-Only the radial-lookup path exists here: particles in one layer at one height,
+``CouplingMatrixVolumeLookupCUDA`` is the drop-in for the reference class of the
+same name (:686-783) for particles at different heights in one layer: 2-D
+(rho, z1 +- z2) tables, interpolated by the sm_103a volume kernel.
+
+Only the lookup paths exist here: particles in one layer,
 ``store_coupling_matrix=False`` and a lookup resolution. Every other branch of
-the reference (explicit coupling, LU, volume lookup, periodic lattices) raises
+the reference (explicit coupling, LU, periodic lattices) raises
 ``NotImplementedError``; nothing falls back to a CPU implementation.
 """
 import sys
@@ -115,6 +119,60 @@ class CouplingMatrixRadialLookupCUDA(CouplingMatrixRadialLookup):
         self.linear_operator = scipy.sparse.linalg.LinearOperator(shape=self.shape, matvec=matvec, dtype=complex)
 
 
+class CouplingMatrixVolumeLookup(SystemMatrix):
+    """Builds the volumetric lookup tables (reference :563-589) for particles in one layer."""
+
+    def __init__(self, vacuum_wavelength, particle_list, layer_system, k_parallel='default', resolution=None,
+                 table_context=None):
+        layers_ = {layer_system.layer_number(p.position[2]) for p in particle_list}
+        if len(layers_) != 1:
+            raise ValueError('the volume lookup needs all particles in one layer')
+        SystemMatrix.__init__(self, particle_list)
+        self.l_max = max(p.l_max for p in particle_list)
+        self.m_max = max(p.m_max for p in particle_list)
+        self.blocksize = flds.blocksize(self.l_max, self.m_max)
+        self.resolution = resolution
+        lkup = look.volumetric_coupling_lookup_table(vacuum_wavelength=vacuum_wavelength, particle_list=particle_list,
+                                                     layer_system=layer_system, k_parallel=k_parallel,
+                                                     resolution=resolution, context=table_context)
+        self.lookup_table_plus, self.lookup_table_minus = lkup[0], lkup[1]
+        self.rho_array, self.sum_z_array, self.diff_z_array = lkup[2], lkup[3], lkup[4]
+
+
+class CouplingMatrixVolumeLookupCUDA(CouplingMatrixVolumeLookup):
+    """GPU volume-lookup coupling matrix W (drop-in for the reference CUDA class, :686-783).
+
+    ``interpolator_kind``: 'linear' (bilinear; the CPU and the CUDA reference agree), 'cubic'
+    (tensor-product not-a-knot spline, the CPU reference's RectBivariateSpline meaning) or
+    'cubic_hermite' (the 4 x 4-tap formula of the reference CUDA kernel). ``cuda_blocksize`` is
+    accepted for signature compatibility.
+    """
+
+    def __init__(self, vacuum_wavelength, particle_list, layer_system, k_parallel='default', resolution=None,
+                 cuda_blocksize=None, interpolator_kind='linear', device=0, context=None):
+        if interpolator_kind not in ('linear', 'cubic', 'cubic_hermite'):
+            raise ValueError('unknown interpolator_kind %r' % interpolator_kind)
+        self.context = context if context is not None else Context(device)
+        CouplingMatrixVolumeLookup.__init__(self, vacuum_wavelength, particle_list, layer_system, k_parallel,
+                                            resolution, table_context=self.context)
+        self.interpolator_kind = interpolator_kind
+        self.unknown_particle, self.unknown_n, self.m_of_n, _, _ = unknown_layout(particle_list)
+        pos = np.array([p.position for p in particle_list], dtype=np.float64)
+        self.context.set_particles(pos[:, :2], self.unknown_particle, self.unknown_n, self.blocksize, self.m_of_n)
+        res = self.rho_array[1] - self.rho_array[0] if self.resolution is None else self.resolution
+        self.context.set_volume_lookup(interpolator_kind, pos[:, 2], self.lookup_table_plus, self.lookup_table_minus,
+                                       self.rho_array[0], self.sum_z_array[0], self.diff_z_array[0], res)
+        self.precision = SG_FP64
+
+        def matvec(v):
+            return self.context.coupling_matvec(np.asarray(v, dtype=complex).ravel(), self.precision)
+
+        self.linear_operator = scipy.sparse.linalg.LinearOperator(shape=self.shape, matvec=matvec, dtype=complex)
+
+
+GPU_COUPLING_MATRICES = (CouplingMatrixRadialLookupCUDA, CouplingMatrixVolumeLookupCUDA)
+
+
 class TMatrix(SystemMatrix):
     """Block-diagonal system T-matrix (reference :410-438)."""
 
@@ -166,8 +224,8 @@ class MasterMatrix(SystemMatrix):
         SystemMatrix.__init__(self, t_matrix.particle_list)
         self.t_matrix = t_matrix
         self.coupling_matrix = coupling_matrix
-        if not isinstance(coupling_matrix, CouplingMatrixRadialLookupCUDA):
-            raise NotImplementedError('only the GPU radial-lookup coupling matrix is provided by smuthi_gb300')
+        if not isinstance(coupling_matrix, GPU_COUPLING_MATRICES):
+            raise NotImplementedError('only the GPU lookup coupling matrices are provided by smuthi_gb300')
         blocks, types, diagonal = t_matrix.device_blocks(coupling_matrix.blocksize, coupling_matrix.l_max,
                                                          coupling_matrix.m_max)
         self.context = coupling_matrix.context
@@ -181,7 +239,8 @@ class MasterMatrix(SystemMatrix):
 
 
 class LinearSystem:
-    """Assemble and solve (1 - T W) b = T a with the GPU radial lookup.
+    """Assemble and solve (1 - T W) b = T a with a GPU lookup (radial, or volume for particles at
+    different heights).
 
     Extra keyword ``precision``: 'fp64' (plain drop-in, default) or 'mixed'
     (FP32 coupling operator inside FP64 iterative refinement; FP64 true
@@ -255,14 +314,20 @@ class LinearSystem:
         if len(layers_) != 1:
             raise NotImplementedError('particles in different layers need the explicit coupling path')
         z = {p.position[2] for p in self.particle_list}
-        if len(z) != 1:
-            raise NotImplementedError('particles at different heights need the volume lookup (not provided)')
         if not cu.use_gpu:
             raise RuntimeError('smuthi_gb300 has no CPU coupling path; GPU use is disabled')
         kind = self.interpolator_kind
         if kind not in ('linear', 'cubic', 'cubic_hermite'):
             warnings.warn(kind + ' interpolation not implemented. Use "linear" instead')
             kind = 'linear'
+        if len(z) != 1:  # not all particles at one height: volume lookup (reference :206-215)
+            sys.stdout.write('Coupling matrix computation by ' + kind + ' interpolation of 3D lookup on GPU.\n')
+            self.coupling_matrix = CouplingMatrixVolumeLookupCUDA(
+                vacuum_wavelength=self.initial_field.vacuum_wavelength, particle_list=self.particle_list,
+                layer_system=self.layer_system, k_parallel=self.k_parallel,
+                resolution=self.coupling_matrix_lookup_resolution, cuda_blocksize=self.cuda_blocksize,
+                interpolator_kind=kind)
+            return
         sys.stdout.write('Coupling matrix computation by ' + kind + ' interpolation of radial lookup on GPU.\n')
         self.coupling_matrix = CouplingMatrixRadialLookupCUDA(
             vacuum_wavelength=self.initial_field.vacuum_wavelength, particle_list=self.particle_list,

@@ -1,6 +1,7 @@
-"""Radial coupling lookup table w[rho, n1, n2] for particles at one height.
+"""Coupling lookup tables: radial w[rho, n1, n2] (particles at one height) and volumetric
+w_pl[rho, z1 + z2, n1, n2], w_mn[rho, z1 - z2, n1, n2] (particles at different heights).
 
-Follows smuthi/linearsystem/particlecoupling/prepare_lookup.py:253-464:
+The radial table follows smuthi/linearsystem/particlecoupling/prepare_lookup.py:253-464:
 
 * radial grid ``arange(-3 r, rho_max + 3 r, r)`` (:291);
 * direct part: sum over ld of a5/b5 (l2, m2, l1, m1, ld) * h_ld(k rho) * P_ld^{|m1-m2|}(0)
@@ -14,6 +15,8 @@ Follows smuthi/linearsystem/particlecoupling/prepare_lookup.py:253-464:
   one complex matrix product per |dm|: the trapezoid weights (dkappa_{k-1} +
   dkappa_k) are folded into the belbe columns;
 * result ``w + wr`` (complex128).
+
+The volumetric tables follow prepare_lookup.py:16-250 (see ``volumetric_coupling_lookup_table``).
 """
 import sys
 
@@ -131,19 +134,7 @@ def layer_mediated_part(vacuum_wavelength, layer_system, i_s, dz, rho, k_paralle
     jac = kp / (kz * k_is)
     wr = np.zeros((len(rho), bs * bs), complex)
     dmat = np.abs(mm[:, None] - mm[None, :])
-    besjac_host = None
-    if context is not None:
-        import torch
-        dev = torch.device("cuda", context.device)
-        stream = torch.cuda.current_stream(dev).cuda_stream
-        kp_d = torch.from_numpy(np.ascontiguousarray(kp, dtype=np.complex128)).to(dev)
-        jac_d = torch.from_numpy(np.ascontiguousarray(jac, dtype=np.complex128)).to(dev)
-        rho_d = torch.from_numpy(np.ascontiguousarray(rho, dtype=np.float64)).to(dev)
-        besjac_dev = torch.empty((2 * m_max + 1, len(rho), len(kp)), dtype=torch.complex128, device=dev)
-        context.bessel_jac_table_dev(kp_d.data_ptr(), jac_d.data_ptr(), len(kp), rho_d.data_ptr(), len(rho),
-                                     2 * m_max, besjac_dev.data_ptr(), stream=stream)
-        besjac_host = besjac_dev.cpu().numpy()
-        del besjac_dev, kp_d, jac_d, rho_d
+    besjac_host = _bessel_factors(kp, jac, rho, 2 * m_max, context)
     for dm in range(2 * m_max + 1):
         n1s, n2s = np.nonzero(dmat == dm)
         if len(n1s) == 0:
@@ -186,3 +177,167 @@ def radial_coupling_lookup_table(vacuum_wavelength, particle_list, layer_system,
     wr = layer_mediated_part(vacuum_wavelength, layer_system, i_s, dz, rho, k_parallel, l_max, m_max,
                              context=context)
     return w + wr, rho
+
+
+def volume_grids(positions, resolution):
+    """(rho, sz, dz) grids of the volume lookup (prepare_lookup.py:57-73) and the smallest lateral
+    particle distance."""
+    pos = np.asarray(positions, dtype=float)
+    dmax, dmin = pair_distance_extremes(pos[:, :2])
+    z = pos[:, 2]
+    rho = np.arange(-3 * resolution, dmax + 3 * resolution, resolution)
+    sz = np.arange(2 * z.min() - 3 * resolution, 2 * z.max() + 3 * resolution, resolution)
+    dz = np.arange(z.min() - z.max() - 3 * resolution, z.max() - z.min() + 3 * resolution, resolution)
+    if len(sz) != len(dz):
+        raise ValueError('volume lookup: z1 + z2 and z1 - z2 grids differ in length')
+    return rho, sz, dz, dmin
+
+
+def direct_part_volume(k_is, rho, dz, l_max, m_max, rho_min_pair):
+    """Direct SVWF coupling on the (rho, z1 - z2) grid in complex64 [len_rho, len_dz, B, B].
+
+    prepare_lookup.py:86-134: per (m1, m2, l1, l2) the sum over ld of a5/b5 * h_ld(k r) *
+    P_ld^{|m1-m2|}(cos theta) with r = sqrt(rho^2 + dz^2) (r = 0 replaced by 1e-20), in the
+    reference's order of operations and rounded once to complex64 like the reference array; zeroed
+    below half the smallest lateral particle distance (:133).
+    """
+    bs = flds.blocksize(l_max, m_max)
+    r = np.sqrt(dz[None, :] ** 2 + rho[:, None] ** 2)
+    r[r == 0] = 1e-20
+    leg, _, _ = legendre_normalized(dz[None, :] / r, rho[:, None] / r, 2 * l_max)
+    hank = [spherical_hankel(n, k_is * r) for n in range(2 * l_max + 1)]
+    w = np.zeros((len(rho), len(dz), bs, bs), dtype=np.complex64)
+    with np.errstate(over='ignore'):  # r = 1e-20 rows overflow complex64; they are zeroed below
+        for m1 in range(-m_max, m_max + 1):
+            for m2 in range(-m_max, m_max + 1):
+                dm = abs(m1 - m2)
+                for l1 in range(max(1, abs(m1)), l_max + 1):
+                    for l2 in range(max(1, abs(m2)), l_max + 1):
+                        A = np.zeros(r.shape, complex)
+                        B = np.zeros(r.shape, complex)
+                        for ld in range(max(abs(l1 - l2), dm), l1 + l2 + 1):
+                            a5, b5 = ab5_coefficients(l2, m2, l1, m1, ld)
+                            A += a5 * hank[ld] * leg[ld, dm]
+                            B += b5 * hank[ld] * leg[ld, dm]
+                        same = [flds.multi_to_single_index(t, l1, m1, l_max, m_max) for t in range(2)]
+                        other = [flds.multi_to_single_index(t, l2, m2, l_max, m_max) for t in range(2)]
+                        for t1 in range(2):
+                            for t2 in range(2):
+                                w[:, :, same[t1], other[t2]] = A if t1 == t2 else B
+    w[rho < rho_min_pair / 2] = 0
+    return w
+
+
+def layer_mediated_volume(vacuum_wavelength, layer_system, i_s, rho, sz, dz, k_parallel, l_max, m_max,
+                          context=None, max_columns=1 << 21):
+    """Layer-mediated volume tables (wr_pl, wr_mn), complex64 [len_rho, len_z, B, B].
+
+    prepare_lookup.py:137-248: per (n1, n2) the trapezoidal Sommerfeld integral
+    2 i^|dm| sum_k (f_k + f_{k+1}) dkappa_k of f = J_dm(kappa rho) kappa/(k_z k) * belbee(z, kappa),
+    with belbee_pl built from the z1 + z2 phases and belbee_mn from the z1 - z2 phases. Here the
+    trapezoid weights are folded into belbee and, per |dm|, every (z, n1, n2) column is one matrix
+    product with the Bessel factors (evaluated on the context's GPU when one is given, as for the
+    radial table); the result is rounded to complex64 like the reference arrays.
+    """
+    k_is = layer_system.wavenumber(i_s, vacuum_wavelength)
+    z_is = layer_system.reference_z(i_s)
+    omega = flds.angular_frequency(vacuum_wavelength)
+    kp = np.asarray(k_parallel)
+    kz = flds.k_z(k_parallel=kp, k=k_is)
+    tau, ll, mm = flds.index_table(l_max, m_max)
+    bs = len(tau)
+    _, pi_pl, ta_pl = legendre_normalized(kz / k_is, kp / k_is, l_max)
+    _, pi_mn, ta_mn = legendre_normalized(-kz / k_is, kp / k_is, l_max)
+    Bd = np.zeros((2, 2, bs, len(kp)), complex)
+    Bn = np.zeros((2, 2, bs, len(kp)), complex)
+    L = np.zeros((2, 2, 2, len(kp)), complex)
+    for pol in range(2):
+        L[pol] = lay.layersystem_response_matrix(pol, layer_system.thicknesses, layer_system.refractive_indices, kp,
+                                                 omega, i_s, i_s)
+        for n in range(bs):
+            Bd[pol, 0, n] = transformation_coefficients_vwf(tau[n], ll[n], mm[n], pol, pi_pl, ta_pl, dagger=True)
+            Bd[pol, 1, n] = transformation_coefficients_vwf(tau[n], ll[n], mm[n], pol, pi_mn, ta_mn, dagger=True)
+            Bn[pol, 0, n] = transformation_coefficients_vwf(tau[n], ll[n], mm[n], pol, pi_pl, ta_pl)
+            Bn[pol, 1, n] = transformation_coefficients_vwf(tau[n], ll[n], mm[n], pol, pi_mn, ta_mn)
+    epl_sz = np.exp(1j * kz[None, :] * (sz[:, None] - 2 * z_is))  # [z, k]
+    emn_sz = np.exp(-1j * kz[None, :] * (sz[:, None] - 2 * z_is))
+    epl_dz = np.exp(1j * kz[None, :] * dz[:, None])
+    emn_dz = np.exp(-1j * kz[None, :] * dz[:, None])
+    dkp = np.diff(kp)
+    wts = np.zeros(len(kp), complex)
+    wts[:-1] += dkp
+    wts[1:] += dkp
+    jac = kp / (kz * k_is)
+    nr, nz = len(rho), len(sz)
+    wr_pl = np.zeros((nr, nz, bs * bs), dtype=np.complex64)
+    wr_mn = np.zeros((nr, nz, bs * bs), dtype=np.complex64)
+    besjac_all = _bessel_factors(kp, jac, rho, 2 * m_max, context)
+    dmat = np.abs(mm[:, None] - mm[None, :])
+    for dm in range(2 * m_max + 1):
+        n1s, n2s = np.nonzero(dmat == dm)
+        if len(n1s) == 0:
+            continue
+        besjac = (besjac_all[dm] if besjac_all is not None
+                  else scipy.special.jv(dm, kp[None, :] * rho[:, None]) * jac[None, :])
+        step = max(1, max_columns // nz)
+        for c0 in range(0, len(n1s), step):
+            a, b = n1s[c0:c0 + step], n2s[c0:c0 + step]
+            # per pair and kappa: coefficients of the four phase terms (prepare_lookup.py:222-229)
+            c_pl_p = np.einsum('pak,pak->ak', L[:, 0, 1][:, None, :] * Bd[:, 0, a], Bn[:, 1, b])
+            c_pl_m = np.einsum('pak,pak->ak', L[:, 1, 0][:, None, :] * Bd[:, 1, a], Bn[:, 0, b])
+            c_mn_p = np.einsum('pak,pak->ak', L[:, 0, 0][:, None, :] * Bd[:, 0, a], Bn[:, 0, b])
+            c_mn_m = np.einsum('pak,pak->ak', L[:, 1, 1][:, None, :] * Bd[:, 1, a], Bn[:, 1, b])
+            cols = a * bs + b
+            for out, cp, cm, ep, em in ((wr_pl, c_pl_p, c_pl_m, epl_sz, emn_sz),
+                                        (wr_mn, c_mn_p, c_mn_m, epl_dz, emn_dz)):
+                G = (cp[None, :, :] * ep[:, None, :] + cm[None, :, :] * em[:, None, :]) * wts[None, None, :]
+                G = G.reshape(nz * len(a), len(kp)).T  # [k, (z, pair)]
+                res = 2 * ipow(dm) * (besjac @ G)  # [rho, (z, pair)]
+                out[:, :, cols] = res.reshape(nr, nz, len(a))
+    return wr_pl.reshape(nr, nz, bs, bs), wr_mn.reshape(nr, nz, bs, bs)
+
+
+def _bessel_factors(kp, jac, rho, nmax, context):
+    """J_n(kappa rho) * jac for n = 0..nmax on the context's GPU ([n, rho, kappa]); None without one."""
+    if context is None:
+        return None
+    import torch
+    dev = torch.device("cuda", context.device)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    kp_d = torch.from_numpy(np.ascontiguousarray(kp, dtype=np.complex128)).to(dev)
+    jac_d = torch.from_numpy(np.ascontiguousarray(jac, dtype=np.complex128)).to(dev)
+    rho_d = torch.from_numpy(np.ascontiguousarray(rho, dtype=np.float64)).to(dev)
+    out = torch.empty((nmax + 1, len(rho), len(kp)), dtype=torch.complex128, device=dev)
+    context.bessel_jac_table_dev(kp_d.data_ptr(), jac_d.data_ptr(), len(kp), rho_d.data_ptr(), len(rho), nmax,
+                                 out.data_ptr(), stream=stream)
+    return out.cpu().numpy()
+
+
+def volumetric_coupling_lookup_table(vacuum_wavelength, particle_list, layer_system, k_parallel='default',
+                                     resolution=None, context=None):
+    """(w_pl, w_mn, rho_grid, sz_grid, dz_grid) for particles at different heights in one layer.
+
+    prepare_lookup.py:16-250: w_pl[rho, z1 + z2, n1, n2] is the layer-mediated coupling indexed by
+    the sum of the heights, w_mn[rho, z1 - z2, n1, n2] the direct plus layer-mediated coupling
+    indexed by their difference; both complex64 like the reference. ``context``: a library context
+    whose GPU evaluates the Bessel factors (None: host scipy).
+    """
+    if resolution is None:
+        resolution = vacuum_wavelength / 100
+        sys.stdout.write('Setting lookup resolution to %f\n' % resolution)
+    l_max = max(p.l_max for p in particle_list)
+    m_max = max(p.m_max for p in particle_list)
+    pos = np.array([p.position for p in particle_list], dtype=float)
+    rho, sz, dz, dmin = volume_grids(pos, resolution)
+    i_s = layer_system.layer_number(pos[0, 2])
+    k_is = layer_system.wavenumber(i_s, vacuum_wavelength)
+    w = direct_part_volume(k_is, rho, dz, l_max, m_max, dmin)
+    if layer_system.is_degenerate():
+        return np.zeros_like(w), w, rho, sz, dz
+    if isinstance(k_parallel, str) and k_parallel == 'default':
+        k_parallel = flds.default_Sommerfeld_k_parallel_array
+    if k_parallel is None:
+        raise ValueError('no Sommerfeld contour: pass k_parallel or set the default contour')
+    wr_pl, wr_mn = layer_mediated_volume(vacuum_wavelength, layer_system, i_s, rho, sz, dz, k_parallel, l_max, m_max,
+                                         context=context)
+    return wr_pl, w + wr_mn, rho, sz, dz

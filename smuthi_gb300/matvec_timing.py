@@ -4,7 +4,12 @@
 
 Builds the seeded sphere ensemble of the shape, applies the operator ``repeat`` times to the
 plane-wave right-hand sides (device buffers, the context's stream) and prints one JSON line with
-the mean CUDA-event time per launch. It is also the small, fixed launch sequence used to profile
+the mean CUDA-event time per launch.
+
+    python -m smuthi_gb300.matvec_timing --volume --n-spheres 1000 --nrhs 16 --precision fp64 --kind linear
+
+times the volume-lookup operator instead: spheres (radius 60 nm) on a jittered 200 nm square
+lattice at seeded heights in [100, 160] nm above a glass substrate, 550 nm, 10 nm lookup grid. It is also the small, fixed launch sequence used to profile
 one coupling kernel: the first operator application carries one-time set-up (pair table, double-float
 coefficients, FP32 kernel autotuning), the later ones are steady state.
 """
@@ -18,6 +23,32 @@ from . import _lib, learned
 PRECISIONS = {"fp64": _lib.SG_FP64, "fp32": _lib.SG_FP32, "df64": _lib.SG_DF64, "tf32x3": _lib.SG_TF32X3}
 
 
+def volume_system(n, nrhs, kind, seed=0):
+    """Spheres at different heights above a substrate with the GPU volume lookup (see module doc)."""
+    from . import fields as flds
+    from . import layers, particles
+    from .linearsystem import linear_system as lsm
+    rng = np.random.default_rng(seed)
+    side = int(np.ceil(np.sqrt(n)))
+    cells = np.array([(a, b) for a in range(side) for b in range(side)][:n], dtype=float)
+    xy = 200.0 * cells + rng.uniform(-20.0, 20.0, size=cells.shape)
+    z = rng.uniform(100.0, 160.0, size=n)
+    parts = [particles.Sphere(position=[x, y, zz], refractive_index=2.0 + 0.02j, radius=60.0, l_max=3, m_max=3)
+             for (x, y), zz in zip(xy, z)]
+    ls = layers.LayerSystem([0, 0], [1.52, 1])
+    wl = 550.0
+    kp = flds.reasonable_Sommerfeld_kpar_contour(wl, layer_refractive_indices=ls.refractive_indices)
+    ctx = _lib.Context(0)
+    W = lsm.CouplingMatrixVolumeLookupCUDA(wl, parts, ls, k_parallel=kp, resolution=10.0, interpolator_kind=kind,
+                                           context=ctx)
+    for p in parts:
+        p.t_matrix = p.compute_t_matrix(wl, ls.refractive_indices[ls.layer_number(p.position[2])])
+    lsm.MasterMatrix(lsm.TMatrix(parts), W)
+    rhs = rng.standard_normal((W.shape[0], nrhs)) + 1j * rng.standard_normal((W.shape[0], nrhs))
+    return dict(ctx=ctx, n=n, blocksize=W.blocksize, rhs=rhs,
+                table_shape=list(W.lookup_table_plus.shape))
+
+
 def main(argv=None):
     import torch
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
@@ -26,8 +57,13 @@ def main(argv=None):
     ap.add_argument("--nrhs", type=int, default=16)
     ap.add_argument("--precision", default="df64", choices=sorted(PRECISIONS))
     ap.add_argument("--repeat", type=int, default=3)
+    ap.add_argument("--volume", action="store_true", help="time the volume lookup (particles at different heights)")
+    ap.add_argument("--kind", default="linear", choices=("linear", "cubic", "cubic_hermite"))
     a = ap.parse_args(argv)
-    system = learned.film_system(a.workload, a.n_spheres, nrhs=a.nrhs)
+    if a.volume:
+        system = volume_system(a.n_spheres or 1000, a.nrhs, a.kind)
+    else:
+        system = learned.film_system(a.workload, a.n_spheres, nrhs=a.nrhs)
     ctx = system["ctx"]
     dev = torch.device("cuda", ctx.device)
     x = torch.from_numpy(np.ascontiguousarray(system["rhs"])).to(dev)
@@ -41,8 +77,12 @@ def main(argv=None):
         ctx.master_matvec_dev(x.data_ptr(), y.data_ptr(), a.nrhs, prec)
     ms, n = ctx.kernel_timing(prec, reset=True)
     ctx.profile(False)
-    print(json.dumps({"workload": a.workload, "n_spheres": system["n"], "blocksize": system["blocksize"],
-                      "nrhs": a.nrhs, "precision": a.precision, "launches": n, "ms_per_launch": ms / max(n, 1)}))
+    out = {"workload": "volume/" + a.kind if a.volume else a.workload, "n_spheres": system["n"],
+           "blocksize": system["blocksize"], "nrhs": a.nrhs, "precision": a.precision, "launches": n,
+           "ms_per_launch": ms / max(n, 1)}
+    if a.volume:
+        out["table_shape"] = system["table_shape"]
+    print(json.dumps(out))
     ctx.close()
 
 

@@ -7,8 +7,10 @@ reference converts every particle's outgoing SWE to a plane wave expansion and
 applies the layer response per particle (scattered_field.py:80-150,
 transformations.py:133-233). For particles in one layer the conversion is
 linear in the particles' coefficients, so here the particle sum is a matrix
-product (coefficients x angular factors x lateral phase) taken before the
-layer response, which is applied once.
+product (coefficients x angular factors x lateral phase, times a per-particle
+height factor when the particles sit at different heights) taken before the
+layer response, which is applied once. Particles with a smaller multipole
+cut-off enter with zeros at the indices they lack.
 """
 import numpy as np
 
@@ -19,24 +21,39 @@ from ..utility.math import legendre_normalized
 
 
 def _particle_data(particle_list, coefficients=None):
-    z = {p.position[2] for p in particle_list}
-    lm = {(p.l_max, p.m_max) for p in particle_list}
-    if len(z) != 1 or len(lm) != 1:
-        raise NotImplementedError('cross sections are provided for particles at one height with one multipole cut-off')
-    l_max, m_max = lm.pop()
-    xy = np.array([p.position[:2] for p in particle_list], dtype=float)
+    """(xy, z, l_max, m_max, coefficients) of the particles.
+
+    z is a scalar when all particles share one height, else the per-particle heights. The
+    coefficients are in the index layout of the largest cut-off (l_max, m_max): [N, B] or, for
+    particles of one cut-off, also [R, N, B]; with mixed cut-offs they come one array per particle
+    (``coefficients`` given as a sequence, or the particles' scattered fields) and are embedded
+    with zeros.
+    """
+    pos = np.array([p.position for p in particle_list], dtype=float)
+    l_max = max(p.l_max for p in particle_list)
+    m_max = max(p.m_max for p in particle_list)
+    zs = pos[:, 2]
+    z = float(zs[0]) if np.all(zs == zs[0]) else zs
     if coefficients is None:
-        coefficients = np.array([p.scattered_field.coefficients for p in particle_list])
-    return xy, z.pop(), l_max, m_max, np.asarray(coefficients)
+        coefficients = [p.scattered_field.coefficients for p in particle_list]
+    if all((p.l_max, p.m_max) == (l_max, m_max) for p in particle_list):
+        return pos[:, :2], z, l_max, m_max, np.asarray(coefficients)
+    out = np.zeros((len(particle_list), flds.blocksize(l_max, m_max)), complex)
+    for i, (p, c) in enumerate(zip(particle_list, coefficients)):
+        tau, ll, mm = flds.index_table(p.l_max, p.m_max)
+        gidx = [flds.multi_to_single_index(t, l, m, l_max, m_max) for t, l, m in zip(tau, ll, mm)]
+        out[i, gidx] = np.asarray(c).ravel()
+    return pos[:, :2], z, l_max, m_max, out
 
 
 def scattered_pwe(vacuum_wavelength, layer_system, xy, z, l_max, m_max, coefs, layer_number, kpar, alpha,
                   chunk=16, context=None):
     """(g_up, g_down) [nrhs, 2, K, A] of the scattered field in ``layer_number``.
 
-    coefs: [nrhs, N, blocksize] outgoing SWE coefficients (or [N, blocksize]). With a library
-    ``context`` (and real ``kpar``) the particle sum runs on that context's GPU (``sg_farfield_sum``,
-    FP64); the angular factors and the layer response stay on the host.
+    coefs: [nrhs, N, blocksize] outgoing SWE coefficients (or [N, blocksize]); z: the particles'
+    common height, or one height per particle. With a library ``context`` (and real ``kpar``) the
+    particle sum runs on that context's GPU (``sg_farfield_sum_heights``, FP64); the angular factors
+    and the layer response stay on the host.
     """
     coefs = np.asarray(coefs)
     single = coefs.ndim == 2
@@ -46,10 +63,11 @@ def scattered_pwe(vacuum_wavelength, layer_system, xy, z, l_max, m_max, coefs, l
     kpar = np.atleast_1d(np.asarray(kpar))
     alpha = np.atleast_1d(np.asarray(alpha, dtype=float))
     omega = flds.angular_frequency(vacuum_wavelength)
-    i_s = layer_system.layer_number(z)
+    heights = np.ndim(z) > 0
+    i_s = layer_system.layer_number(z[0] if heights else z)
     k = omega * layer_system.refractive_indices[i_s]
     kz = flds.k_z(k_parallel=kpar, k=k)
-    dz = layer_system.reference_z(i_s) - z
+    dz = layer_system.reference_z(i_s) - np.asarray(z)  # scalar, or [N] for particles at different heights
     tau, ll, mm = flds.index_table(l_max, m_max)
     nm = 2 * m_max + 1
     gs = []
@@ -71,14 +89,20 @@ def scattered_pwe(vacuum_wavelength, layer_system, xy, z, l_max, m_max, coefs, l
         for n in range(len(tau)):
             for pol in range(2):
                 S[n, pol, :, mm[n] + m_max] = transformation_coefficients_vwf(tau[n], ll[n], mm[n], pol, pilm, taulm)
-        pref = np.exp(1j * sgn * kz * dz) / (2 * np.pi * kz * k)
+        if heights:
+            pref = 1 / (2 * np.pi * kz * k)
+            zph = np.exp(1j * sgn * kz[:, None] * dz[None, :])  # [K, N]
+        else:
+            pref = np.exp(1j * sgn * kz * dz) / (2 * np.pi * kz * k)
+            zph = None
         if context is not None:
             Sn = np.ascontiguousarray(S[np.arange(len(tau)), :, :, mm + m_max])  # [n, pol, K]
             S_d = torch.from_numpy(Sn).to(dev)
+            zph_d = None if zph is None else torch.from_numpy(np.ascontiguousarray(zph)).to(dev)
             out = torch.empty((R, 2, len(kpar), len(alpha)), dtype=torch.complex128, device=dev)
             context.farfield_sum_dev(N, xy_d.data_ptr(), len(tau), R, c_d.data_ptr(), m_max, mm, len(kpar),
                                      kp_d.data_ptr(), S_d.data_ptr(), len(alpha), al_d.data_ptr(), out.data_ptr(),
-                                     stream=stream)
+                                     stream=stream, zphase_ptr=None if zph_d is None else zph_d.data_ptr())
             gs.append(out.cpu().numpy() * pref[None, None, :, None])
             continue
         D = np.einsum('rin,npkm->rpkmi', coefs, S)  # [R, 2, K, m, N]
@@ -89,6 +113,8 @@ def scattered_pwe(vacuum_wavelength, layer_system, xy, z, l_max, m_max, coefs, l
             kp = kpar[ks]
             ph = np.exp(-1j * kp[:, None, None] * (np.cos(alpha)[None, :, None] * xy[None, None, :, 0]
                                                    + np.sin(alpha)[None, :, None] * xy[None, None, :, 1]))
+            if zph is not None:
+                ph = ph * zph[ks][:, None, :]
             # sum over particles, then over m
             F = np.einsum('kai,rpkmi->rpkam', ph, D[:, :, ks])
             g[:, :, ks, :] = np.einsum('rpkam,ma->rpka', F, eima)

@@ -36,6 +36,10 @@ CASES = {
     "c2s": dict(shape="c2", n=120, kinds=("cubic",), full_table=False, solve_kinds=("cubic",)),
     "c3s": dict(shape="c3", n=40, kinds=("cubic",), full_table=False, solve_kinds=("cubic",)),
     "c5s": dict(shape="c5", n=60, kinds=("linear",), full_table=False, solve_kinds=("linear",)),
+    # particles at different heights above a substrate: the reference takes its volume lookup
+    # (CouplingMatrixVolumeLookupCPU, linear_system.py:592-667) with 2-D (rho, z1 +- z2) tables
+    "vol5": dict(custom="vol5", kinds=("linear", "cubic"), full_table=False, solve_kinds=("linear", "cubic"),
+                 volume=True),
 }
 PARITY_TOL = 1e-13
 
@@ -51,6 +55,18 @@ def _geometry(case, part, lay, init):
         resolution = 5.0
         contour = dict(neff_waypoints=[0, 0.5, 0.8 - 0.01j, 2 - 0.01j, 2.5, 5], neff_resolution=1e-2)
         ref_point = [200, 200, 200]
+    elif case.get("custom") == "vol5":
+        spheres = [dict(position=[0, 0, 100], refractive_index=2.0 + 0.05j, radius=70, l_max=3, m_max=3),
+                   dict(position=[190, 40, 130], refractive_index=2.0 + 0.05j, radius=70, l_max=3, m_max=3),
+                   dict(position=[-60, 200, 90], refractive_index=1.8 + 0.0j, radius=60, l_max=3, m_max=2),
+                   dict(position=[250, 280, 160], refractive_index=2.0 + 0.05j, radius=70, l_max=3, m_max=3),
+                   dict(position=[-230, -150, 120], refractive_index=2.0 + 0.05j, radius=70, l_max=3, m_max=3)]
+        layers = ([0, 0], [1.52, 1])
+        wl = 550.0
+        waves = [(np.pi, 0.0, 0), (np.pi * 5 / 6, 0.7, 1)]
+        resolution = 10.0
+        contour = dict()
+        ref_point = [0, 0, 0]
     else:
         spec = workloads.scaled(case["shape"], case["n"])
         spec = workloads.build(spec, seed=0)
@@ -109,9 +125,27 @@ def run_case(name, case):
             t_run = time.time() - t0
             lsys = sim.linear_system
             cm = lsys.coupling_matrix
-            assert type(cm).__name__ == 'CouplingMatrixRadialLookupCPU'
+            volume = case.get("volume", False)
+            assert type(cm).__name__ == ('CouplingMatrixVolumeLookupCPU' if volume else
+                                         'CouplingMatrixRadialLookupCPU')
             tag = "%s_w%d" % (kind, iw)
             if iw == 0:
+                if volume and "kpar" not in out:
+                    out["kpar"] = np.array(flds.default_Sommerfeld_k_parallel_array)
+                    out["rho_grid"] = cm.rho_array
+                    out["sz_grid"] = cm.sum_z_array
+                    out["dz_grid"] = cm.diff_z_array
+                    for key, tab in (("plus", cm.lookup_table_plus), ("minus", cm.lookup_table_minus)):
+                        out["table_%s_dtype" % key] = np.array(str(tab.dtype))
+                        out["table_%s_shape" % key] = np.array(tab.shape)
+                        rows = np.unique(np.concatenate([np.arange(0, 8), rng.choice(len(tab), size=6,
+                                                                                   replace=False)]))
+                        out["table_%s_rows" % key] = rows
+                        out["table_%s_subset" % key] = tab[rows]
+                        out["table_%s_abs_sum" % key] = np.abs(tab.astype(complex)).sum()
+                        wts = np.cos(0.37 * np.arange(tab.size)).reshape(tab.shape)
+                        out["table_%s_weighted_sum" % key] = (tab.astype(complex) * wts).sum()
+                    out["t_diag"] = np.concatenate([np.diag(p.t_matrix) for p in plist])
                 if "kpar" not in out:
                     out["kpar"] = np.array(flds.default_Sommerfeld_k_parallel_array)
                     out["rho_grid"] = cm.radial_distance_array

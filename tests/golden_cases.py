@@ -10,8 +10,10 @@ import oracle.special as osp
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def available():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz"))
+def available(volume=False):
+    """Fixture names: the radial-lookup cases, or (``volume=True``) the volume-lookup cases."""
+    names = sorted(f[:-4] for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz"))
+    return [n for n in names if n.startswith("vol") == volume]
 
 
 def load(name):
