@@ -218,6 +218,20 @@ int sg_farfield_sum(sg_context *ctx, int n_particles, const void *xy, int blocks
                     int m_max, const int32_t *m_of_n, int nk, const void *kpar, const void *S, int na,
                     const void *alpha, void *out, void *stream);
 
+/* Electric (field = 0) or magnetic (field = 1) field of a plane-wave expansion at n_points points,
+ * replacing the GPU branches of PlaneWaveExpansion.electric_field / magnetic_field
+ * (smuthi/fields/expansions.py:660-708, 734-770; FP32 kernels of smuthi/fields/expansions_cuda.py:5-421):
+ *   F(r) = 1/omega_F int dkappa kappa int dalpha sum_pol g_pol(kappa, alpha) Phi_pol e^{i k.r}
+ * with the reference's trapezoid rules over the alpha grid and the (complex) kappa contour;
+ * omega_F = 1 for E and omega for H. Device buffers: x, y, z float64[n_points] relative to the
+ * expansion's reference point; kpar, kz complex128[nk] (kz signed by the expansion's kind: + upgoing,
+ * - downgoing); alpha float64[na]; g complex128[2][nk][na] (TE, TM); out complex128[3][n_points]
+ * (x, y, z components). k = k_re + i k_im is the medium's wavenumber. nk >= 2, 2 <= na <= 8192.
+ * FP64 throughout. Synchronous on `stream` (NULL = the context's stream). */
+int sg_pwe_field(sg_context *ctx, int field, int n_points, const void *x, const void *y, const void *z, int nk,
+                 const void *kpar, const void *kz, int na, const void *alpha, const void *g, double k_re, double k_im,
+                 double omega, void *out, void *stream);
+
 /* The same for particles at different heights: zphase complex128[nk][n_particles] (device) multiplies
  * particle i's term at kpar_k (exp(+-i k_z (z_ref - z_i)) of the up- or downgoing expansion; the
  * reference applies it per particle in smuthi/fields/transformations.py:133-233). NULL = no factor. */

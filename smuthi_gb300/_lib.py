@@ -31,7 +31,7 @@ EXPORTS = ("sg_last_error", "sg_version", "sg_create", "sg_destroy", "sg_set_par
            "sg_coupling_matvec_linear_noalloc", "sg_precond_param_count", "sg_precond_add_graph",
            "sg_precond_select", "sg_precond_clear", "sg_precond_set_params", "sg_precond_get_params",
            "sg_precond_apply_dev", "sg_precond_train_step", "sg_precond_export_blocks", "sg_bessel_jac_table",
-           "sg_farfield_sum", "sg_set_volume_lookup", "sg_farfield_sum_heights")
+           "sg_farfield_sum", "sg_set_volume_lookup", "sg_farfield_sum_heights", "sg_pwe_field")
 
 
 class LibraryMissing(RuntimeError):
@@ -91,6 +91,7 @@ def _declare(L):
         "sg_bessel_jac_table": [_P, _P, _P, _I, _P, _I, _I, _P, _P],
         "sg_farfield_sum": [_P, _I, _P, _I, _I, _P, _I, _P, _I, _P, _P, _I, _P, _P, _P],
         "sg_farfield_sum_heights": [_P, _I, _P, _I, _I, _P, _I, _P, _I, _P, _P, _I, _P, _P, _P, _P],
+        "sg_pwe_field": [_P, _I, _I, _P, _P, _P, _I, _P, _P, _I, _P, _P, _D, _D, _D, _P, _P],
         "sg_precond_param_count": [_I],
         "sg_precond_add_graph": [_P, _I, _P, ctypes.POINTER(_I)],
         "sg_precond_select": [_P, _I],
@@ -306,6 +307,15 @@ class Context:
         check(lib().sg_bessel_jac_table(self.h, ctypes.c_void_p(kappa_ptr), ctypes.c_void_p(jac_ptr), int(nk),
                                         ctypes.c_void_p(rho_ptr), int(nr), int(nmax), ctypes.c_void_p(out_ptr),
                                         ctypes.c_void_p(stream or 0)))
+
+    def pwe_field_dev(self, field, n, x_ptr, y_ptr, z_ptr, nk, kpar_ptr, kz_ptr, na, alpha_ptr, g_ptr, k, omega,
+                      out_ptr, stream=None):
+        """Field (0 = E, 1 = H) of a plane-wave expansion at n points (device buffers, see the header)."""
+        check(lib().sg_pwe_field(self.h, int(field), int(n), ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr),
+                                 ctypes.c_void_p(z_ptr), int(nk), ctypes.c_void_p(kpar_ptr), ctypes.c_void_p(kz_ptr),
+                                 int(na), ctypes.c_void_p(alpha_ptr), ctypes.c_void_p(g_ptr), float(np.real(k)),
+                                 float(np.imag(k)), float(omega), ctypes.c_void_p(out_ptr),
+                                 ctypes.c_void_p(stream or 0)))
 
     def farfield_sum_dev(self, n, xy_ptr, bs, nrhs, coef_ptr, m_max, m_of_n, nk, kpar_ptr, S_ptr, na, alpha_ptr,
                          out_ptr, stream=None, zphase_ptr=None):

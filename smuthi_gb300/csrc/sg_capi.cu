@@ -637,6 +637,20 @@ int sg_farfield_sum(sg_context *ctx, int n_particles, const void *xy, int blocks
                                  nullptr, out, stream);
 }
 
+int sg_pwe_field(sg_context *ctx, int field, int n_points, const void *x, const void *y, const void *z, int nk,
+                 const void *kpar, const void *kz, int na, const void *alpha, const void *g, double k_re, double k_im,
+                 double omega, void *out, void *stream) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx && x && y && z && kpar && kz && alpha && g && out, "null argument");
+    use_device(ctx);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    ctx->launches += sg::pwe_field(field, n_points, (const double *)x, (const double *)y, (const double *)z, nk,
+                                   (const double2 *)kpar, (const double2 *)kz, na, (const double *)alpha,
+                                   (const double2 *)g, make_double2(k_re, k_im), omega, (double2 *)out, st);
+    return SG_OK;
+  });
+}
+
 int sg_precond_param_count(int blocksize) {
   if (blocksize < 1 || blocksize > 64) return -1;
   return sg::precond_param_count(blocksize);

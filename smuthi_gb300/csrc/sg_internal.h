@@ -141,6 +141,11 @@ void build_volume_table(int kind, const double2 *raw, int len_rho, int len_z, in
 // y = W x or x - T W x with the volume lookup on padded vectors; returns the number of kernels launched
 int launch_volume(sg_context *c, const double2 *x, double2 *y, int R, bool master, bool fp32, cudaStream_t st);
 
+// field of a plane-wave expansion at points (sg_nearfield.cu); synchronous, returns kernels launched
+int pwe_field(int field, int np, const double *x, const double *y, const double *z, int nk, const double2 *kp,
+              const double2 *kz, int na, const double *alpha, const double2 *g, double2 k, double omega, double2 *out,
+              cudaStream_t st);
+
 // Bessel factors of the layer-mediated lookup table (sg_table.cu)
 void bessel_jac_table(const double2 *kp, const double2 *jac, int nk, const double *rho, int nr, int nmax,
                       double2 *out, cudaStream_t st);

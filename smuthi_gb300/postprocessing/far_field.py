@@ -47,13 +47,14 @@ def _particle_data(particle_list, coefficients=None):
 
 
 def scattered_pwe(vacuum_wavelength, layer_system, xy, z, l_max, m_max, coefs, layer_number, kpar, alpha,
-                  chunk=16, context=None):
+                  chunk=16, context=None, include_direct=True, include_layer_response=True):
     """(g_up, g_down) [nrhs, 2, K, A] of the scattered field in ``layer_number``.
 
     coefs: [nrhs, N, blocksize] outgoing SWE coefficients (or [N, blocksize]); z: the particles'
     common height, or one height per particle. With a library ``context`` (and real ``kpar``) the
     particle sum runs on that context's GPU (``sg_farfield_sum_heights``, FP64); the angular factors
-    and the layer response stay on the host.
+    and the layer response stay on the host. ``include_direct`` / ``include_layer_response`` select
+    the two parts as in the reference (scattered_field.py:125-148).
     """
     coefs = np.asarray(coefs)
     single = coefs.ndim == 2
@@ -122,10 +123,10 @@ def scattered_pwe(vacuum_wavelength, layer_system, xy, z, l_max, m_max, coefs, l
     g_up, g_dn = gs
     out_up = np.zeros_like(g_up)
     out_dn = np.zeros_like(g_dn)
-    if i_s == layer_number:
+    if i_s == layer_number and include_direct:
         out_up += g_up
         out_dn += g_dn
-    for pol in range(2):
+    for pol in range(2 if include_layer_response else 0):
         L = lay.layersystem_response_matrix(pol, layer_system.thicknesses, layer_system.refractive_indices, kpar,
                                             omega, i_s, layer_number)
         out_up[:, pol] += L[0, 0][None, :, None] * g_up[:, pol] + L[0, 1][None, :, None] * g_dn[:, pol]

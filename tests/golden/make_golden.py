@@ -39,8 +39,11 @@ CASES = {
     # particles at different heights above a substrate: the reference takes its volume lookup
     # (CouplingMatrixVolumeLookupCPU, linear_system.py:592-667) with 2-D (rho, z1 +- z2) tables
     "vol5": dict(custom="vol5", kinds=("linear", "cubic"), full_table=False, solve_kinds=("linear", "cubic"),
-                 volume=True),
+                 volume=True, near_field=True),
 }
+# plane-wave expansions with seeded coefficients, evaluated by the reference's CPU field code
+# (smuthi/fields/expansions.py:635-900, cpu_precision='double precision')
+PWE_CASES = ("pwe1",)
 PARITY_TOL = 1e-13
 
 
@@ -179,16 +182,66 @@ def run_case(name, case):
                 print("  %s: run %.1fs, cross sections %.1fs, relres %.2e, ext %.6e sca %.6e"
                       % (tag, t_run, time.time() - t1, out["relres_" + tag], out["sigma_ext_" + tag],
                          out["sigma_sca_" + tag]), flush=True)
+                if case.get("near_field") and tag == case["kinds"][0] + "_w0":
+                    # scattered field above the particles from its plane-wave expansion in the top layer
+                    # (smuthi/postprocessing/scattered_field.py:80-150)
+                    import smuthi.postprocessing.scattered_field as sf
+                    i_top = ls.number_of_layers() - 1
+                    pu, pd = sf.scattered_field_pwe(wl, plist, ls, i_top)
+                    pts = np.stack([np.linspace(-300, 400, 6), np.linspace(250, -150, 6),
+                                    np.linspace(320, 520, 6)], axis=1)
+                    out["nf_points"] = pts
+                    out["nf_azimuthal_angles"] = np.array(pu.azimuthal_angles)
+                    out["nf_kpar"] = np.array(pu.k_parallel)
+                    for nm, pwe in (("up", pu), ("down", pd)):
+                        e = pwe.electric_field(pts[:, 0], pts[:, 1], pts[:, 2], cpu_precision='double precision')
+                        out["nf_E_" + nm] = np.array(e)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path) // 1024, "KiB", flush=True)
+
+
+def run_pwe_case(name):
+    """Seeded PlaneWaveExpansion objects (complex contour, both kinds) and their E and H fields."""
+    refload.import_reference()
+    import smuthi.fields as flds
+    import smuthi.fields.expansions as fldex
+    rng = np.random.Generator(np.random.PCG64(77))
+    wl = 550.0
+    k = flds.angular_frequency(wl) * (1.3 + 0.02j)
+    kpar = flds.reasonable_Sommerfeld_kpar_contour(wl, layer_refractive_indices=[1.3 + 0.02j, 1.0],
+                                                    neff_resolution=2e-2)
+    alpha = np.linspace(0, 2 * np.pi, 37)
+    pts = np.stack([rng.uniform(-400, 400, 9), rng.uniform(-400, 400, 9), rng.uniform(-50, 350, 9)], axis=1)
+    out = dict(wavelength=wl, k=k, kpar=kpar, alpha=alpha, points=pts,
+               versions=np.array(["numpy " + np.__version__, "scipy " + scipy.__version__]))
+    for kind, ref, lo, hi in (("upgoing", [10.0, -20.0, 30.0], 0.0, np.inf),
+                              ("downgoing", [-15.0, 5.0, 250.0], -np.inf, 300.0)):
+        pwe = fldex.PlaneWaveExpansion(k=k, k_parallel=kpar, azimuthal_angles=alpha, kind=kind,
+                                       reference_point=ref, lower_z=lo, upper_z=hi)
+        decay = np.exp(-np.abs(kpar) / abs(k))[None, :, None]
+        pwe.coefficients = decay * (rng.standard_normal(pwe.coefficients.shape)
+                                    + 1j * rng.standard_normal(pwe.coefficients.shape))
+        out["g_" + kind] = pwe.coefficients
+        out["ref_" + kind] = np.array(ref)
+        out["bounds_" + kind] = np.array([lo, hi])
+        out["E_" + kind] = np.array(pwe.electric_field(pts[:, 0], pts[:, 1], pts[:, 2],
+                                                       cpu_precision='double precision'))
+        out["H_" + kind] = np.array(pwe.magnetic_field(pts[:, 0], pts[:, 1], pts[:, 2], wl,
+                                                       cpu_precision='double precision'))
     path = os.path.join(HERE, name + ".npz")
     np.savez_compressed(path, **out)
     print("wrote", path, os.path.getsize(path) // 1024, "KiB", flush=True)
 
 
 def main(argv):
-    names = argv or list(CASES)
+    names = argv or list(CASES) + list(PWE_CASES)
     for n in names:
         print("case", n, flush=True)
-        run_case(n, CASES[n])
+        if n in PWE_CASES:
+            run_pwe_case(n)
+        else:
+            run_case(n, CASES[n])
 
 
 if __name__ == "__main__":

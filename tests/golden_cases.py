@@ -11,8 +11,9 @@ GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def available(volume=False):
-    """Fixture names: the radial-lookup cases, or (``volume=True``) the volume-lookup cases."""
-    names = sorted(f[:-4] for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz"))
+    """Fixture names: the radial-lookup solve cases, or (``volume=True``) the volume-lookup cases.
+    (``pwe*`` fixtures hold plane-wave expansions only and are loaded by name.)"""
+    names = sorted(f[:-4] for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz") and not f.startswith("pwe"))
     return [n for n in names if n.startswith("vol") == volume]
 
 
