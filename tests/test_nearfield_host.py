@@ -109,3 +109,22 @@ def test_pwe_algebra():
     a.set_reference_point([3.0, -1.0, 2.0])
     a.set_reference_point([0, 0, 0])
     assert np.allclose(a.coefficients, 1)
+
+
+def test_reference_point_translation_keeps_the_field():
+    """Moving an expansion's reference point rephases its coefficients so that the field at every point
+    is unchanged (the property of the reference's test_pwe_translation.py, here exact up to rounding
+    because the quadrature nodes do not change)."""
+    from smuthi_gb300.fields.expansions import PlaneWaveExpansion
+    g = gc.load("pwe1")
+    pts = g["points"]
+    for kind in ("upgoing", "downgoing"):
+        lo, hi = g["bounds_" + kind]
+        p = PlaneWaveExpansion(complex(g["k"]), g["kpar"], g["alpha"], kind=kind,
+                               reference_point=list(g["ref_" + kind]), lower_z=lo, upper_z=hi)
+        p.coefficients = g["g_" + kind].copy()
+        p.set_reference_point([300.0, 260.0, 100.0])
+        o = onf.PlaneWaveExpansion(p.k, p.k_parallel, p.azimuthal_angles, kind, p.reference_point, lo, hi)
+        o.coefficients = p.coefficients
+        E = np.array(o.field(pts[:, 0], pts[:, 1], pts[:, 2], 'E'))
+        assert gc.relerr(E, g["E_" + kind]) < 1e-9
