@@ -317,7 +317,7 @@ def run_ours(args, rank, world, local_rank):
                         "precond_fallbacks": infos[-1]["precond_fallbacks"],
                         "residual_arithmetic": args.residual,
                         "batched": True, "x0": "0",
-                        "fp32_kernel": dict(zip(("variant", "rhs_tile", "ms_per_receiver", "ms_bucketed"),
+                        "fp32_kernel": dict(zip(("variant", "rhs_tile", "ms_per_receiver", "ms_bucketed", "ms_symmetric"),
                                                 ctx.fp32_autotune(R))),
                         "fp32_kernel_variants": "0 = per-receiver (RHS tile autotuned), 1 = interval-bucketed"},
         "prep_s": round(prep_s, 2),

@@ -168,13 +168,22 @@ int sg_kernel_timing(sg_context *ctx, int precision, double *total_ms, int64_t *
 int sg_launch_count(sg_context *ctx, int64_t *count);
 
 /* FP32-operator autotuner result for an RHS count: variant 0 = per-receiver kernel, 1 =
- * interval-bucketed kernel, -1 = not tuned yet; rhs_tile = the per-receiver kernel's RHS tile per
- * CTA; with the CUDA-event times (ms) of one run of the best per-receiver tile and of the bucketed
- * kernel (-1 when it is not a candidate). The first FP32 application for a new RHS count times the
- * per-receiver kernel at up to three RHS tiles and the bucketed kernel on the live operands
- * (synchronising the stream) and keeps the fastest. No counterpart in the reference. */
+ * interval-bucketed kernel, 2 = pair-symmetric kernel (one interpolation per unordered pair serves
+ * both directions), -1 = not tuned yet; rhs_tile = the chosen kernel's RHS tile per CTA; with the
+ * CUDA-event times (ms) of one run of the best per-receiver tile, of the bucketed kernel and of the
+ * best pair-symmetric tile (-1 when not a candidate). The first FP32 application for a new RHS count
+ * times every candidate on the live operands (synchronising the stream) and keeps the fastest. No
+ * counterpart in the reference. */
 int sg_fp32_autotune(sg_context *ctx, int nrhs, int *variant, int *rhs_tile, double *ms_receiver,
-                     double *ms_bucket);
+                     double *ms_bucket, double *ms_symmetric);
+
+/* Fixes the FP32 operator for an RHS count instead of timing the candidates: variant 0 =
+ * per-receiver kernel (rhs_tile 1, 2, 4, 8 or 16 dividing nrhs), 1 = interval-bucketed kernel
+ * (rhs_tile ignored; needs its plan), 2 = pair-symmetric kernel (rhs_tile a power of two dividing
+ * nrhs, at most 16 for blocksize <= 32 and 8 for blocksize <= 64). Replaces an earlier choice for
+ * that RHS count; set_particles / set_lookup clear it. For tests and measurements of one kernel; no
+ * counterpart in the reference. */
+int sg_fp32_set_kernel(sg_context *ctx, int nrhs, int variant, int rhs_tile);
 
 /* FMA throughput (TFLOP/s, 2 flops per FMA) of the FP64 or FP32 pipe of the
  * context's device, measured with a dependent-chain probe kernel. Used to
@@ -188,11 +197,14 @@ int sg_measure_fma_peak(sg_context *ctx, int precision, double *tflops);
  * positions, m_of_n = int32[blocksize], table = complex128[len_rho][blocksize][blocksize] on the
  * grid rho_k = rho_min + k * resolution (the reference layout; it must cover every particle
  * distance), x, y = complex128[n_particles][blocksize][nrhs] (uniform blocks). The call allocates
- * nothing: its scratch is a static 16 MiB device array held by every device that loads the
- * library until exit, so n_particles * blocksize * nrhs must be <= 1048576 (larger sizes return
- * SG_ERR_ARG). The first call on a device looks the array up (do it before any stream capture);
- * `device` must be the current device. Calls that overlap on the GPU race on the shared scratch.
- * Asynchronous on `stream` (a cudaStream_t, NULL = legacy default stream). */
+ * nothing: its scratch is a static 16 MiB device array, so n_particles * blocksize * nrhs must be
+ * <= 1048576 and nrhs <= 65535 (larger sizes return SG_ERR_ARG). CUDA loads device code lazily:
+ * the first call on a device (and the first after a cudaDeviceReset) loads the code holding the
+ * array, which allocates its 16 MiB then and keeps them until exit, and looks its address up. Make
+ * that first call at start-up, before a memory pool claims the device and before any stream
+ * capture; later calls allocate nothing. `device` must be the current device. Every call shares the
+ * array: calls that overlap on the GPU race on it. Asynchronous on `stream` (a cudaStream_t, NULL =
+ * legacy default stream). */
 int sg_coupling_matvec_linear_noalloc(int device, int n_particles, const void *xy, int blocksize,
                                       const void *m_of_n, int len_rho, double rho_min, double resolution,
                                       const void *table, const void *x, void *y, int nrhs, void *stream);

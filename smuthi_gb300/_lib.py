@@ -27,7 +27,7 @@ KINDS = {"linear": SG_LINEAR, "cubic": SG_CUBIC, "cubic_hermite": SG_CUBIC_HERMI
 EXPORTS = ("sg_last_error", "sg_version", "sg_create", "sg_destroy", "sg_set_particles", "sg_set_lookup",
            "sg_set_tmatrix", "sg_coupling_matvec", "sg_master_matvec", "sg_coupling_matvec_dev",
            "sg_master_matvec_dev", "sg_gmres_solve", "sg_gmres_solve_dev", "sg_true_residual", "sg_profile",
-           "sg_kernel_timing", "sg_launch_count", "sg_measure_fma_peak", "sg_fp32_autotune",
+           "sg_kernel_timing", "sg_launch_count", "sg_measure_fma_peak", "sg_fp32_autotune", "sg_fp32_set_kernel",
            "sg_coupling_matvec_linear_noalloc", "sg_precond_param_count", "sg_precond_add_graph",
            "sg_precond_select", "sg_precond_clear", "sg_precond_set_params", "sg_precond_get_params",
            "sg_precond_apply_dev", "sg_precond_train_step", "sg_precond_export_blocks", "sg_bessel_jac_table",
@@ -86,7 +86,9 @@ def _declare(L):
         "sg_kernel_timing": [_P, _I, ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_int64), _I],
         "sg_launch_count": [_P, ctypes.POINTER(ctypes.c_int64)],
         "sg_measure_fma_peak": [_P, _I, ctypes.POINTER(_D)],
-        "sg_fp32_autotune": [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D)],
+        "sg_fp32_autotune": [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D),
+                             ctypes.POINTER(_D)],
+        "sg_fp32_set_kernel": [_P, _I, _I, _I],
         "sg_coupling_matvec_linear_noalloc": [_I, _I, _P, _I, _P, _I, _D, _D, _P, _P, _P, _I, _P],
         "sg_bessel_jac_table": [_P, _P, _P, _I, _P, _I, _I, _P, _P],
         "sg_farfield_sum": [_P, _I, _P, _I, _I, _P, _I, _P, _I, _P, _P, _I, _P, _P, _P],
@@ -253,15 +255,21 @@ class Context:
         return out.value
 
     def fp32_autotune(self, nrhs):
-        """(variant, RHS tile, ms best per-receiver tile, ms bucketed) for an RHS count; variant -1 if not
-        tuned yet, ms bucketed -1 when that kernel is not a candidate."""
+        """(variant, RHS tile, ms best per-receiver tile, ms bucketed, ms best pair-symmetric tile) for an
+        RHS count; variant -1 if not tuned yet (0 per-receiver, 1 bucketed, 2 pair-symmetric), a time is
+        -1 when that kernel is not a candidate."""
         v = ctypes.c_int()
         t = ctypes.c_int()
         a = ctypes.c_double()
         b = ctypes.c_double()
+        c = ctypes.c_double()
         check(lib().sg_fp32_autotune(self.h, int(nrhs), ctypes.byref(v), ctypes.byref(t), ctypes.byref(a),
-                                     ctypes.byref(b)))
-        return v.value, t.value, a.value, b.value
+                                     ctypes.byref(b), ctypes.byref(c)))
+        return v.value, t.value, a.value, b.value, c.value
+
+    def fp32_set_kernel(self, nrhs, variant, rhs_tile=0):
+        """Fix the FP32 operator for an RHS count (0 per-receiver, 1 bucketed, 2 pair-symmetric)."""
+        check(lib().sg_fp32_set_kernel(self.h, int(nrhs), int(variant), int(rhs_tile)))
 
     # -- learned preconditioner
     def precond_add_graph(self, nbr):

@@ -401,6 +401,8 @@ static int matvec_host(sg_context *ctx, const double *x, double *y, int nrhs, in
     matvec_dev(ctx, ctx->io_in.ptr, ctx->io_out.ptr, nrhs, precision, master, st);
     SG_CUDA(cudaMemcpyAsync(y, ctx->io_out.ptr, len * sizeof(double2), cudaMemcpyDeviceToHost, st));
     SG_CUDA(cudaStreamSynchronize(st));
+    if (precision == SG_FP32 && sg::sym_check_error(ctx, st))
+      throw sg::Error{SG_ERR_CUDA, "pair-symmetric FP32 operator: a bounded wait ran out"};
     return SG_OK;
   });
 }
@@ -471,6 +473,8 @@ static int solve_dev_impl(sg_context *ctx, const double2 *b, double2 *x, int nrh
     ctx->launches += 1;
   }
   if (info) *info = local;
+  if ((precision & SG_FP32) && sg::sym_check_error(ctx, st))
+    throw sg::Error{SG_ERR_CUDA, "pair-symmetric FP32 operator: a bounded wait ran out"};
   if (!std::isfinite(local.max_rel_residual)) throw sg::Error{SG_ERR_NAN, "solver produced NaN or Inf"};
   if (local.converged < nrhs) {
     sg::set_error("GMRES did not reach the tolerance for every right-hand side");
@@ -586,18 +590,52 @@ int sg_measure_fma_peak(sg_context *ctx, int precision, double *tflops) {
 }
 
 int sg_fp32_autotune(sg_context *ctx, int nrhs, int *variant, int *rhs_tile, double *ms_receiver,
-                     double *ms_bucket) {
+                     double *ms_bucket, double *ms_symmetric) {
   return guarded([&]() -> int {
     SG_REQUIRE(ctx && variant, "null argument");
     for (const auto &t : ctx->tuned)
       if (t.nrhs == nrhs) {
         *variant = t.variant;
-        if (rhs_tile) *rhs_tile = t.rt;
+        if (rhs_tile) *rhs_tile = t.variant == 2 ? t.sym_rt : t.rt;
         if (ms_receiver) *ms_receiver = t.ms_receiver;
         if (ms_bucket) *ms_bucket = t.ms_bucket;
+        if (ms_symmetric) *ms_symmetric = t.ms_sym;
         return SG_OK;
       }
     *variant = -1;
+    return SG_OK;
+  });
+}
+
+int sg_fp32_set_kernel(sg_context *ctx, int nrhs, int variant, int rhs_tile) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx, "null context");
+    SG_REQUIRE(nrhs >= 1, "nrhs must be >= 1");
+    SG_REQUIRE(!ctx->vol && ctx->kind >= 0, "a radial lookup must be set");
+    SG_REQUIRE(variant >= 0 && variant <= 2, "variant must be 0, 1 or 2");
+    use_device(ctx);
+    ensure_pairs(ctx, ctx->stream);  // builds the FP32 operator data now (it would clear the choice later)
+    sg_context::Tuned t{nrhs, variant, 0, -1.f, -1.f, 0, -1.f};
+    if (variant == 0) {
+      SG_REQUIRE(rhs_tile == 1 || rhs_tile == 2 || rhs_tile == 4 || rhs_tile == 8 || rhs_tile == 16,
+                 "per-receiver RHS tile must be 1, 2, 4, 8 or 16");
+      SG_REQUIRE(nrhs % rhs_tile == 0, "RHS tile must divide nrhs");
+      t.rt = rhs_tile;
+    } else if (variant == 1) {
+      SG_REQUIRE(ctx->use_bucket, "the bucketed kernel has no plan for this geometry");
+    } else {
+      SG_REQUIRE(sg::sym_supported(ctx), "the pair-symmetric kernel needs blocksize <= 64");
+      SG_REQUIRE(rhs_tile >= 1 && rhs_tile <= sg::sym_max_tile(ctx) && (rhs_tile & (rhs_tile - 1)) == 0,
+                 "pair-symmetric RHS tile must be a power of two within the kernel's register budget");
+      SG_REQUIRE(nrhs % rhs_tile == 0, "RHS tile must divide nrhs");
+      t.sym_rt = rhs_tile;
+    }
+    for (auto &e : ctx->tuned)
+      if (e.nrhs == nrhs) {
+        e = t;
+        return SG_OK;
+      }
+    ctx->tuned.push_back(t);
     return SG_OK;
   });
 }

@@ -1105,10 +1105,31 @@ static int autotune_fp32(sg_context *c, const double2 *x, double2 *y, int R, boo
   }
   float ms_bucket = -1.f;
   if (c->use_bucket) ms_bucket = time_it([&] { c->launches += launch_bucket_matvec(c, x, y, R, master, st); });
+  // the pair-symmetric kernel at the two largest RHS tiles that divide R within its register budget
+  float ms_sym = -1.f;
+  int sym_rt = 0;
+  if (sym_supported(c)) {
+    int ntile = 0;
+    for (int rt : {16, 8, 4, 2, 1}) {
+      if (rt > sym_max_tile(c) || R % rt != 0 || ntile == 2) continue;
+      ++ntile;
+      const float ms = time_it([&] { c->launches += launch_sym_matvec(c, x, y, R, master, rt, st); });
+      if (ms_sym < 0.f || ms < ms_sym) {
+        ms_sym = ms;
+        sym_rt = rt;
+      }
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  const int v = (ms_bucket >= 0.f && ms_bucket < best_rec) ? 1 : 0;
-  c->tuned.push_back({R, v, best_rt, best_rec, ms_bucket});
+  int v = 0;
+  float best = best_rec;
+  if (ms_bucket >= 0.f && ms_bucket < best) {
+    v = 1;
+    best = ms_bucket;
+  }
+  if (ms_sym >= 0.f && ms_sym < best) v = 2;
+  c->tuned.push_back({R, v, best_rt, best_rec, ms_bucket, sym_rt, ms_sym});
   return v;
 }
 
@@ -1119,7 +1140,7 @@ void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool maste
     SG_CUDA(cudaEventCreate(&e1));
     SG_CUDA(cudaEventRecord(e0, st));
   }
-  int variant = 0, rt = 0;
+  int variant = 0, rt = 0, sym_rt = 0;
   if (c->vol) {
     c->launches += launch_volume(c, x, y, R, master, fp32, st);
     variant = -1;
@@ -1129,13 +1150,17 @@ void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool maste
       if (t.nrhs == R) {
         variant = t.variant;
         rt = t.rt;
+        sym_rt = t.sym_rt;
       }
     if (variant < 0) {
       variant = autotune_fp32(c, x, y, R, master, st);
       rt = c->tuned.back().rt;
+      sym_rt = c->tuned.back().sym_rt;
     }
   }
-  if (variant == 1) {
+  if (variant == 2) {
+    c->launches += launch_sym_matvec(c, x, y, R, master, sym_rt, st);
+  } else if (variant == 1) {
     c->launches += launch_bucket_matvec(c, x, y, R, master, st);
   } else if (variant == 0) {
     CouplingLaunch L{};

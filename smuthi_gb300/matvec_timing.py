@@ -59,6 +59,9 @@ def main(argv=None):
     ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--volume", action="store_true", help="time the volume lookup (particles at different heights)")
     ap.add_argument("--kind", default="linear", choices=("linear", "cubic", "cubic_hermite"))
+    ap.add_argument("--fp32-kernel", default=None, metavar="VARIANT:TILE",
+                    help="fix the FP32 kernel (0 per-receiver, 1 bucketed, 2 pair-symmetric) and its RHS tile "
+                         "instead of the autotuner's choice")
     a = ap.parse_args(argv)
     if a.volume:
         system = volume_system(a.n_spheres or 1000, a.nrhs, a.kind)
@@ -69,6 +72,9 @@ def main(argv=None):
     x = torch.from_numpy(np.ascontiguousarray(system["rhs"])).to(dev)
     y = torch.empty_like(x)
     prec = PRECISIONS[a.precision]
+    if a.fp32_kernel:
+        v, t = (int(s) for s in a.fp32_kernel.split(":"))
+        ctx.fp32_set_kernel(a.nrhs, v, t)
     ctx.master_matvec_dev(x.data_ptr(), y.data_ptr(), a.nrhs, prec)  # set-up and warm-up
     torch.cuda.synchronize(dev)
     ctx.profile(True)
@@ -82,6 +88,9 @@ def main(argv=None):
            "ms_per_launch": ms / max(n, 1)}
     if a.volume:
         out["table_shape"] = system["table_shape"]
+    if a.precision == "fp32" and not a.volume:
+        out["fp32_kernel"] = dict(zip(("variant", "rhs_tile", "ms_per_receiver", "ms_bucketed", "ms_symmetric"),
+                                      ctx.fp32_autotune(a.nrhs)))
     print(json.dumps(out))
     ctx.close()
 
