@@ -5,8 +5,12 @@
 // host loop with a fixed memory budget that must not allocate after start-up. For them,
 // sg_coupling_matvec_linear_noalloc takes every input and output as caller-owned device buffers
 // and keeps its scratch -- the per-split partial sums of the emitter-split coupling kernel -- in
-// the file-scope static device array below (16 MiB, allocated once when the library is loaded
-// onto a device and held by every device that loads the library until the process exits).
+// the file-scope static device array below (16 MiB, held by every device that loads it until the
+// process exits). CUDA loads a library's device code lazily: the 16 MiB are allocated when this
+// file's code is first loaded onto a device, which is inside the first call of this entry point
+// on that device (the address lookup below). A caller whose memory pool claims the device's memory
+// must therefore make one call at start-up, before the pool takes the memory and before any stream
+// capture; later calls on that device allocate nothing.
 //
 // The scratch array is shared by all calls: it keeps the last call's contents, every call
 // overwrites the part it reads before reading it, and calls whose executions overlap on the GPU
@@ -25,24 +29,43 @@ static __device__ __align__(256) double2 g_noalloc_scratch[kNoAllocScratchElems]
 
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
-double2 *g_scratch_ptr[kMaxDevices] = {};
+struct ScratchAddr {
+  void *ctx;     // CUDA context the address belongs to
+  double2 *ptr;  // device address of g_noalloc_scratch in that context
+};
+ScratchAddr g_scratch[kMaxDevices] = {};
 
-// Device address of the static scratch on `device` (looked up once per device with that device
-// current; the first call on a device therefore performs this set-up and should come before any
-// stream capture).
+// The calling thread's current CUDA context (a driver call, reached through the runtime so that the
+// library links only the runtime); null when it cannot be resolved.
+void *current_context() {
+  typedef int (*GetCurrentFn)(void **);
+  static GetCurrentFn fn = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<GetCurrentFn>(f);
+  }();
+  void *ctx = nullptr;
+  if (fn && fn(&ctx) != 0) ctx = nullptr;
+  return ctx;
+}
+
+// Device address of the static scratch on `device`, which must be current. Looked up once per
+// device and context: the first call on a device (or after a cudaDeviceReset replaced its context)
+// performs this set-up, which loads the module holding the array.
 double2 *scratch_on(int device) {
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (g_scratch_ptr[device]) return g_scratch_ptr[device];
-  int prev = 0;
-  SG_CUDA(cudaGetDevice(&prev));
-  if (prev != device) SG_CUDA(cudaSetDevice(device));
+  void *ctx = current_context();
+  if (g_scratch[device].ptr && ctx && g_scratch[device].ctx == ctx) return g_scratch[device].ptr;
   void *p = nullptr;
   cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-  if (prev != device) cudaSetDevice(prev);
   if (e != cudaSuccess)
     throw sg::Error{SG_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e)};
-  g_scratch_ptr[device] = reinterpret_cast<double2 *>(p);
-  return g_scratch_ptr[device];
+  if (ctx == nullptr) ctx = current_context();  // the lookup initialised the context
+  g_scratch[device] = {ctx, reinterpret_cast<double2 *>(p)};
+  return g_scratch[device].ptr;
 }
 
 constexpr int kThreads = 256;
@@ -162,6 +185,7 @@ extern "C" int sg_coupling_matvec_linear_noalloc(int device, int n_particles, co
   sg::clear_error();
   try {
     SG_REQUIRE(n_particles >= 1 && blocksize >= 1 && blocksize <= 96 && nrhs >= 1, "bad sizes");
+    SG_REQUIRE(nrhs <= 65535, "nrhs must be <= 65535 (one grid row per right-hand side)");
     SG_REQUIRE(len_rho >= 2 && resolution > 0, "bad lookup grid");
     SG_REQUIRE(xy && m_of_n && table && x && y, "null buffer");
     SG_REQUIRE(device >= 0 && device < kMaxDevices, "device index out of range");
