@@ -8,6 +8,10 @@ GMRES(20) with x0 = b, one RHS) is timed on the same GPU and reported beside
 it. ``e2e`` repeats the chosen-form step through the public C ABI with host
 (pinned) buffers, host<->device copies inside the timed region.
 
+At one GPU the line also carries a ``target`` block: the 10 000-sphere film (16 plane waves) solved
+once with the chosen form and once (first wave) with the plain FP64 drop-in, in the same run
+(``--target none`` skips it; it takes several minutes, most of them in the plain FP64 solve).
+
 ``--impl reference`` times the reference's CPU path (the oracle restatement
 of ``CouplingMatrixRadialLookupCPU``) on a bounded sample of the same
 workload and extrapolates to seconds per RHS. Multi-GPU runs (torchrun) are
@@ -319,7 +323,9 @@ def run_ours(args, rank, world, local_rank):
                         "batched": True, "x0": "0",
                         "fp32_kernel": dict(zip(("variant", "rhs_tile", "ms_per_receiver", "ms_bucketed", "ms_symmetric"),
                                                 ctx.fp32_autotune(R))),
-                        "fp32_kernel_variants": "0 = per-receiver (RHS tile autotuned), 1 = interval-bucketed"},
+                        "fp32_kernel_variants": "0 = per-receiver, 1 = interval-bucketed, 2 = pair-symmetric (one warp per "
+                                                "receiver), 3 = pair-symmetric (two warps per receiver); RHS tile "
+                                                "autotuned"},
         "prep_s": round(prep_s, 2),
         "e2e": {"value": round(e2e_value, 6), "unit": UNIT, "h2d_bytes_per_step": int(2 * rhs.nbytes),
                 "d2h_bytes_per_step": int(rhs.nbytes)},
@@ -333,8 +339,97 @@ def run_ours(args, rank, world, local_rank):
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    table = PLAIN_FP64_MATVECS.get(args.workload)
+    line["plain_fp64"]["matvecs_used_by_reference_arm"] = table
+    line["plain_fp64"]["reference_arm_count_consistent"] = table == pinfo.fp64_matvecs
     ctx.close()
+    if world == 1 and args.target != "none":
+        line["target"] = run_target(args, local_rank)
     return line
+
+
+# ----------------------------------------------------------------------------------------- target
+def run_target(args, local_rank):
+    """The target configuration measured once in the same run: the chosen form on the 10 000-sphere film
+    (16 plane waves) against the plain FP64 drop-in on its first wave, both to an FP64-true relative
+    residual of 1e-6 on the same GPU. Warm-up: one application of every operator the solves use (the
+    pair table, the double-float coefficients, the FP32 autotuning and the preconditioner's near-field
+    blocks are built on first use); the timed solves then run once each (a chosen-form solve takes
+    minutes, the plain one several)."""
+    import torch
+    from smuthi_gb300 import _lib, learned
+    from smuthi_gb300.linearsystem import linear_system as lsm
+    name = args.target
+    R = 16
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    t0 = time.time()
+    wl = make_workload(name, R)
+    spec = wl["spec"]
+    ctx = _lib.Context(local_rank)
+    W = lsm.CouplingMatrixRadialLookupCUDA(wl["wl"], wl["parts"], wl["ls"], k_parallel=wl["kpar"],
+                                           resolution=spec["resolution"], interpolator_kind=spec["kind"],
+                                           context=ctx)
+    lsm.MasterMatrix(lsm.TMatrix(wl["parts"]), W)
+    n, bs = spec["n_spheres"], W.blocksize
+    prec = _lib.SG_FP32 | _lib.SG_DF64
+    pname = "precond_%s" % name
+    if os.path.exists(os.path.join(learned.DATA_DIR, pname + ".npz")):
+        learned.attach(ctx, np.array([p.position[:2] for p in wl["parts"]]), bs, learned.load_params(pname, bs),
+                       k=learned.load_meta(pname)["k"])
+        prec |= _lib.SG_PRECOND
+    else:
+        pname = None
+    rhs = wl["rhs"]
+    b_dev = torch.from_numpy(rhs).to(dev)
+    x_dev = torch.zeros_like(b_dev)
+    tmp = torch.empty_like(b_dev)
+    sp = torch.cuda.current_stream(dev).cuda_stream
+    for p in (_lib.SG_FP32, _lib.SG_DF64):
+        ctx.master_matvec_dev(b_dev.data_ptr(), tmp.data_ptr(), R, p, stream=sp)
+    if pname:
+        ctx.precond_apply_dev(b_dev.data_ptr(), tmp.data_ptr(), R, stream=sp)
+    torch.cuda.synchronize(dev)
+    prep_s = time.time() - t0
+    stream = torch.cuda.current_stream(dev)
+    clocks = ClockSampler(local_rank)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    info = ctx.gmres_dev(b_dev.data_ptr(), x_dev.data_ptr(), R, TOL, restart=args.restart, maxiter=0,
+                         precision=prec, stream=sp)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    chosen_s = e0.elapsed_time(e1) / 1e3
+    relres = ctx.true_residual(rhs, np.ascontiguousarray(x_dev.cpu().numpy()))
+    b0 = torch.from_numpy(np.ascontiguousarray(rhs[:, 0])).to(dev)
+    x0 = b0.clone()
+    e0.record(stream)
+    pinfo = ctx.gmres_dev(b0.data_ptr(), x0.data_ptr(), 1, TOL, restart=20, maxiter=0, precision=_lib.SG_FP64,
+                          stream=sp)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    plain_s = e0.elapsed_time(e1) / 1e3
+    clk = clocks.stop()
+    prelres = ctx.true_residual(rhs[:, 0], np.ascontiguousarray(x0.cpu().numpy()))
+    out = {"workload": name, "n_spheres": n, "blocksize": bs, "unknowns": n * bs, "nrhs": R,
+           "interpolation": spec["kind"],
+           "chosen_form": {"s_per_rhs": round(chosen_s / R, 4), "solve_s": round(chosen_s, 3),
+                           "iterations": info.iterations, "refinement_steps": info.restarts,
+                           "fp32_matvecs": info.fp32_matvecs, "fp64_grade_matvecs": info.fp64_matvecs,
+                           "max_rel_residual_fp64": float(relres.max()), "learned_preconditioner": pname,
+                           "precond_fallbacks": info.precond_fallbacks, "residual_arithmetic": "df64",
+                           "fp32_kernel": dict(zip(("variant", "rhs_tile", "ms_per_receiver", "ms_bucketed",
+                                                    "ms_symmetric"), ctx.fp32_autotune(R)))},
+           "plain_fp64": {"s_per_rhs": round(plain_s, 3), "iterations": pinfo.iterations,
+                          "fp64_matvecs": pinfo.fp64_matvecs, "rel_residual_fp64": float(prelres[0]),
+                          "restart": 20, "x0": "b"},
+           "speedup_vs_plain_fp64": round(plain_s / (chosen_s / R), 2),
+           "met": bool(relres.max() <= TOL * 1.0001 and prelres[0] <= TOL * 1.0001),
+           "prep_s": round(prep_s, 1), "clocks": clk,
+           "warmup": "one application of the FP32 and double-float operators and the preconditioner (one-time "
+                     "set-up and autotuning); each solve timed once with CUDA events"}
+    ctx.close()
+    return out
 
 
 # ----------------------------------------------------------------------------------------- CPU reference
@@ -452,6 +547,8 @@ def main(argv=None):
                     help="learned-preconditioner weights name, 'none', or 'auto' (precond_<workload> if shipped)")
     ap.add_argument("--residual", default="df64", choices=["df64", "fp64"],
                     help="arithmetic of the refinement's true residuals")
+    ap.add_argument("--target", default="c5", choices=["c5", "c3", "c2", "none"],
+                    help="configuration of the one-shot target block (1 GPU only): chosen form vs plain FP64")
     args = ap.parse_args(argv)
     rank, world, local_rank = dist_env()
     if world > 1:

@@ -256,8 +256,8 @@ class Context:
 
     def fp32_autotune(self, nrhs):
         """(variant, RHS tile, ms best per-receiver tile, ms bucketed, ms best pair-symmetric tile) for an
-        RHS count; variant -1 if not tuned yet (0 per-receiver, 1 bucketed, 2 pair-symmetric), a time is
-        -1 when that kernel is not a candidate."""
+        RHS count; variant -1 if not tuned yet (0 per-receiver, 1 bucketed, 2 pair-symmetric, 3 pair-symmetric
+        with two warps per receiver), a time is -1 when that kernel is not a candidate."""
         v = ctypes.c_int()
         t = ctypes.c_int()
         a = ctypes.c_double()
@@ -268,7 +268,8 @@ class Context:
         return v.value, t.value, a.value, b.value, c.value
 
     def fp32_set_kernel(self, nrhs, variant, rhs_tile=0):
-        """Fix the FP32 operator for an RHS count (0 per-receiver, 1 bucketed, 2 pair-symmetric)."""
+        """Fix the FP32 operator for an RHS count (0 per-receiver, 1 bucketed, 2 pair-symmetric, 3 pair-symmetric
+        with two warps per receiver)."""
         check(lib().sg_fp32_set_kernel(self.h, int(nrhs), int(variant), int(rhs_tile)))
 
     # -- learned preconditioner

@@ -596,7 +596,7 @@ int sg_fp32_autotune(sg_context *ctx, int nrhs, int *variant, int *rhs_tile, dou
     for (const auto &t : ctx->tuned)
       if (t.nrhs == nrhs) {
         *variant = t.variant;
-        if (rhs_tile) *rhs_tile = t.variant == 2 ? t.sym_rt : t.rt;
+        if (rhs_tile) *rhs_tile = t.variant >= 2 ? t.sym_rt : t.rt;
         if (ms_receiver) *ms_receiver = t.ms_receiver;
         if (ms_bucket) *ms_bucket = t.ms_bucket;
         if (ms_symmetric) *ms_symmetric = t.ms_sym;
@@ -612,7 +612,7 @@ int sg_fp32_set_kernel(sg_context *ctx, int nrhs, int variant, int rhs_tile) {
     SG_REQUIRE(ctx, "null context");
     SG_REQUIRE(nrhs >= 1, "nrhs must be >= 1");
     SG_REQUIRE(!ctx->vol && ctx->kind >= 0, "a radial lookup must be set");
-    SG_REQUIRE(variant >= 0 && variant <= 2, "variant must be 0, 1 or 2");
+    SG_REQUIRE(variant >= 0 && variant <= 3, "variant must be 0, 1, 2 or 3");
     use_device(ctx);
     ensure_pairs(ctx, ctx->stream);  // builds the FP32 operator data now (it would clear the choice later)
     sg_context::Tuned t{nrhs, variant, 0, -1.f, -1.f, 0, -1.f};
@@ -628,6 +628,7 @@ int sg_fp32_set_kernel(sg_context *ctx, int nrhs, int variant, int rhs_tile) {
       SG_REQUIRE(rhs_tile >= 1 && rhs_tile <= sg::sym_max_tile(ctx) && (rhs_tile & (rhs_tile - 1)) == 0,
                  "pair-symmetric RHS tile must be a power of two within the kernel's register budget");
       SG_REQUIRE(nrhs % rhs_tile == 0, "RHS tile must divide nrhs");
+      SG_REQUIRE(variant == 2 || rhs_tile >= 4, "two warps per receiver need an RHS tile >= 4");
       t.sym_rt = rhs_tile;
     }
     for (auto &e : ctx->tuned)

@@ -1105,18 +1105,23 @@ static int autotune_fp32(sg_context *c, const double2 *x, double2 *y, int R, boo
   }
   float ms_bucket = -1.f;
   if (c->use_bucket) ms_bucket = time_it([&] { c->launches += launch_bucket_matvec(c, x, y, R, master, st); });
-  // the pair-symmetric kernel at the two largest RHS tiles that divide R within its register budget
+  // the pair-symmetric kernel at the two largest RHS tiles that divide R within its register budget,
+  // with one warp per receiver and (tiles >= 4) with two
   float ms_sym = -1.f;
-  int sym_rt = 0;
+  int sym_rt = 0, sym_split = 1;
   if (sym_supported(c)) {
     int ntile = 0;
     for (int rt : {16, 8, 4, 2, 1}) {
       if (rt > sym_max_tile(c) || R % rt != 0 || ntile == 2) continue;
       ++ntile;
-      const float ms = time_it([&] { c->launches += launch_sym_matvec(c, x, y, R, master, rt, st); });
-      if (ms_sym < 0.f || ms < ms_sym) {
-        ms_sym = ms;
-        sym_rt = rt;
+      for (int split : {1, 2}) {
+        if (split == 2 && rt < 4) continue;
+        const float ms = time_it([&] { c->launches += launch_sym_matvec(c, x, y, R, master, rt, split, st); });
+        if (ms_sym < 0.f || ms < ms_sym) {
+          ms_sym = ms;
+          sym_rt = rt;
+          sym_split = split;
+        }
       }
     }
   }
@@ -1128,7 +1133,7 @@ static int autotune_fp32(sg_context *c, const double2 *x, double2 *y, int R, boo
     v = 1;
     best = ms_bucket;
   }
-  if (ms_sym >= 0.f && ms_sym < best) v = 2;
+  if (ms_sym >= 0.f && ms_sym < best) v = sym_split == 2 ? 3 : 2;
   c->tuned.push_back({R, v, best_rt, best_rec, ms_bucket, sym_rt, ms_sym});
   return v;
 }
@@ -1158,8 +1163,8 @@ void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool maste
       sym_rt = c->tuned.back().sym_rt;
     }
   }
-  if (variant == 2) {
-    c->launches += launch_sym_matvec(c, x, y, R, master, sym_rt, st);
+  if (variant == 2 || variant == 3) {
+    c->launches += launch_sym_matvec(c, x, y, R, master, sym_rt, variant == 3 ? 2 : 1, st);
   } else if (variant == 1) {
     c->launches += launch_bucket_matvec(c, x, y, R, master, st);
   } else if (variant == 0) {

@@ -115,7 +115,8 @@ int launch_bucket_matvec(sg_context *c, const double2 *x, double2 *y, int R, boo
 // pair-symmetric FP32 operator (sg_sym.cu): each unordered pair's interpolated block serves both directions
 bool sym_supported(const sg_context *c);
 int sym_max_tile(const sg_context *c);
-int launch_sym_matvec(sg_context *c, const double2 *x, double2 *y, int R, bool master, int rt, cudaStream_t st);
+int launch_sym_matvec(sg_context *c, const double2 *x, double2 *y, int R, bool master, int rt, int split,
+                      cudaStream_t st);
 bool sym_check_error(sg_context *c, cudaStream_t st);  // reads and clears the timeout flag (synchronises)
 // FP32 per-pair data (interval index, t, cos, sin) for all ordered pairs.
 void build_pairs(const double2 *pos, int n, double rho_min, double res, int n_int, int4 *pairs, cudaStream_t st);
@@ -215,11 +216,11 @@ struct sg_context {
   // FP32 kernel autotuner: per RHS count, the fastest of the per-receiver, the bucketed and the
   // pair-symmetric kernel
   struct Tuned {
-    int nrhs, variant;  // 0 per-receiver, 1 bucketed, 2 pair-symmetric
+    int nrhs, variant;  // 0 per-receiver, 1 bucketed, 2 pair-symmetric, 3 pair-symmetric (2 warps per receiver)
     int rt;             // per-receiver kernel: RHS tile per CTA
     float ms_receiver, ms_bucket;  // best per-receiver tile, bucketed (< 0: not a candidate)
     int sym_rt;         // pair-symmetric kernel: RHS tile per CTA
-    float ms_sym;       // best pair-symmetric tile (< 0: not a candidate)
+    float ms_sym;       // best pair-symmetric tile and layout (< 0: not a candidate)
   };
   std::vector<Tuned> tuned;
   std::vector<std::pair<int, int>> tuned_df;  // double-float kernel: (nrhs, RHS tile)
@@ -230,7 +231,7 @@ struct sg_context {
   sg::DevBuf<double2> bk_yacc;
   // pair-symmetric FP32 operator: work items (receiver tile, emitter-tile run) and FP32 accumulator
   sg::DevBuf<int4> sym_items;
-  int sym_n_items = 0, sym_items_n = -1;
+  int sym_n_items = 0, sym_items_n = -1, sym_items_T = 0;
   sg::DevBuf<float2> sym_yacc;
   sg::DevBuf<int> sym_err;  // set when a bounded wait of the pair-symmetric kernel ran out
   bool sym_err_init = false;

@@ -2,7 +2,8 @@
 
 The FP32 operator drives the correction solves of the mixed-precision refinement; the autotuner
 picks among the per-receiver kernel (RHS tiles 1-16), the interval-bucketed kernel and the
-pair-symmetric kernel (one interpolation per unordered pair for both directions). Each is fixed
+pair-symmetric kernel (one interpolation per unordered pair for both directions, with one or two warps
+per receiver). Each is fixed
 here with ``fp32_set_kernel`` and compared, through the C ABI, with the FP64 operator (relative
 2-norm 2e-5, the FP32 bound the other FP32 tests use) and with the reference's W x / M x.
 Also: the full (non-diagonal) T-matrix epilogue of the FP64, per-receiver FP32 and pair-symmetric
@@ -23,6 +24,7 @@ def _variants(ctx, R, bs):
     """(variant, tile) pairs the library accepts for R right-hand sides."""
     out = [(0, t) for t in (1, 2, 4, 8, 16) if R % t == 0]
     out += [(2, t) for t in (1, 2, 4, 8, 16) if R % t == 0 and t <= (16 if bs <= 32 else 8)]
+    out += [(3, t) for t in (4, 8, 16) if R % t == 0 and t <= (16 if bs <= 32 else 8)]
     return out
 
 
@@ -76,7 +78,7 @@ def test_full_t_epilogue(name, gpu_context):
         wx = gpu_context.coupling_matvec(X, _lib.SG_FP64).reshape(n, bs, R)
         ref = (Xr - np.einsum("iab,ibr->iar", blocks[types], wx)).reshape(X.shape)
         assert gc.relerr(gpu_context.master_matvec(X, _lib.SG_FP64), ref) < 1e-13
-        for v, t in [(0, 1), (2, 1)] + ([(0, 4), (2, 4)] if R == 4 else []):
+        for v, t in [(0, 1), (2, 1)] + ([(0, 4), (2, 4), (3, 4)] if R == 4 else []):
             gpu_context.fp32_set_kernel(R, v, t)
             assert gc.relerr(gpu_context.master_matvec(X, _lib.SG_FP32), ref) < TOL32, (R, v, t)
 
@@ -85,7 +87,7 @@ def test_fp32_set_kernel_rejects_bad_choices(gpu_context):
     from smuthi_gb300 import _lib
     g = gc.load("c1")
     _product_system(g, "linear", gpu_context)
-    for args in [(16, 0, 3), (4, 0, 8), (16, 2, 32), (6, 2, 4), (4, 5, 1)]:
+    for args in [(16, 0, 3), (4, 0, 8), (16, 2, 32), (6, 2, 4), (4, 5, 1), (2, 3, 2)]:
         with pytest.raises(_lib.SmuthiGB300Error) as e:
             gpu_context.fp32_set_kernel(*args)
         assert e.value.code == _lib.SG_ERR_ARG
@@ -110,6 +112,8 @@ def test_full_size_c2_symmetric_kernel(gpu_context):
     y64 = gpu_context.coupling_matvec(X, _lib.SG_FP64)
     gpu_context.fp32_set_kernel(16, 2, 16)
     ys = gpu_context.coupling_matvec(X, _lib.SG_FP32)
+    gpu_context.fp32_set_kernel(16, 3, 16)
+    assert gc.relerr(gpu_context.coupling_matvec(X, _lib.SG_FP32), y64) < TOL32
     gpu_context.fp32_set_kernel(16, 0, 8)
     yr = gpu_context.coupling_matvec(X, _lib.SG_FP32)
     assert gc.relerr(ys, y64) < TOL32
@@ -120,5 +124,5 @@ def test_full_size_c2_symmetric_kernel(gpu_context):
     yt = gpu_context.coupling_matvec(X, _lib.SG_FP32)
     assert gc.relerr(yt, y64) < TOL32
     variant, tile, ms_rec, ms_bucket, ms_sym = gpu_context.fp32_autotune(16)
-    assert variant in (0, 1, 2) and ms_rec > 0 and ms_sym > 0
+    assert variant in (0, 1, 2, 3) and ms_rec > 0 and ms_sym > 0
     del W2
