@@ -126,3 +126,32 @@ def test_full_size_c2_symmetric_kernel(gpu_context):
     variant, tile, ms_rec, ms_bucket, ms_sym = gpu_context.fp32_autotune(16)
     assert variant in (0, 1, 2, 3) and ms_rec > 0 and ms_sym > 0
     del W2
+
+
+def test_full_size_c3_operator_and_mixed_solve(gpu_context):
+    """5000 spheres, blocksize 48, cubic lookup at 2 nm (the mixed-precision shape at full size): FP64
+    operator rows against the oracle, every FP32 kernel against FP64, and the chosen form's solve of
+    four plane waves to an FP64-true relative residual of 1e-6."""
+    import oracle.physics as ophys
+    import oracle.solve as osv
+    from smuthi_gb300 import _lib, learned
+    system = learned.film_system("c3", nrhs=4, ctx=gpu_context)
+    W, n, bs = system["W"], system["n"], system["blocksize"]
+    assert (n, bs) == (5000, 48)
+    rng = np.random.default_rng(13)
+    x = rng.standard_normal(W.shape[0]) + 1j * rng.standard_normal(W.shape[0])
+    y = gpu_context.coupling_matvec(x, _lib.SG_FP64)
+    rows = np.array([0, 2500, 4999])
+    oparts = [ophys.Sphere(p.position, p.refractive_index, p.radius, p.l_max, p.m_max) for p in system["parts"]]
+    Wo = osv.RadialLookupCPU(oparts, W.lookup_table, W.radial_distance_array, "cubic")
+    yo = Wo.matvec(x, rows=rows)
+    sel = np.concatenate([np.arange(r * bs, (r + 1) * bs) for r in rows])
+    assert gc.relerr(y[sel], yo[sel]) < 1e-11
+    X = np.ascontiguousarray(system["rhs"])
+    y64 = gpu_context.coupling_matvec(X, _lib.SG_FP64)
+    for v, t in [(0, 4), (2, 4), (3, 4)]:
+        gpu_context.fp32_set_kernel(4, v, t)
+        assert gc.relerr(gpu_context.coupling_matvec(X, _lib.SG_FP32), y64) < TOL32, (v, t)
+    sol, info = gpu_context.gmres(X, np.zeros_like(X), 1e-6, restart=64, precision=_lib.SG_FP32 | _lib.SG_DF64)
+    assert info.converged == 4
+    assert gpu_context.true_residual(X, sol).max() <= 1e-6
