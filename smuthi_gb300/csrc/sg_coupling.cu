@@ -390,7 +390,7 @@ static void launch_r(const CouplingLaunch &L, int nsplit, cudaStream_t st) {
 }
 
 int choose_split(int n_particles, int nrhs) {
-  const int target = 2 * 152;
+  const int target = 2 * sm_count();
   int s = (target + n_particles - 1) / n_particles;
   if (s < 1) s = 1;
   const int maxs = n_particles / 8 > 0 ? n_particles / 8 : 1;  // keep >= 8 emitters per CTA

@@ -170,7 +170,7 @@ struct Solver {
     int p2 = 1;
     while (p2 * 2 <= tpr) p2 *= 2;
     tpb = p2 * R;
-    const int nblk = (int)std::min<size_t>(152 * 2, (rows + p2 - 1) / p2);
+    const int nblk = (int)std::min<size_t>((size_t)sm_count() * 2, (rows + p2 - 1) / p2);
     c->w_tmp.reserve((size_t)nblk * nvec * R);
     dots_partial_kernel<<<nblk, tpb, tpb * sizeof(double2), st>>>(V, nvec, w, rows, R, c->w_tmp.ptr);
     SG_CUDA(cudaGetLastError());
@@ -587,7 +587,7 @@ struct BlockOps {
   // H[i] (Ra x Ra) = V_i^H W for i < nv, result on the host (row-major [i][a][b])
   void gram(const VecList &V, int nv, const double2 *W, int Ra, std::vector<cd> &H) {
     const int ntile = (Ra + 15) / 16;
-    const int nblk = (int)std::min<size_t>(152, (rows + 31) / 32);
+    const int nblk = (int)std::min<size_t>((size_t)sm_count(), (rows + 31) / 32);
     const size_t n = (size_t)nv * Ra * Ra;
     c->w_tmp.reserve((size_t)nblk * n + n);
     dim3 grid(nblk, nv, ntile * ntile);

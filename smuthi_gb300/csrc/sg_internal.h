@@ -137,6 +137,19 @@ inline bool first_on_device(bool (&done)[64]) {
   return true;
 }
 
+// number of SMs of the current device (queried once per device; grid sizes scale with it)
+inline int sm_count() {
+  static int cache[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+  if (cache[dev] == 0) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v < 1) v = 1;
+    cache[dev] = v;
+  }
+  return cache[dev];
+}
+
 // FMA-throughput probe (TFLOP/s) of the FP64 or FP32 pipe
 double fma_peak(int fp64, cudaStream_t st);
 

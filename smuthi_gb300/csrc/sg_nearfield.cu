@@ -172,7 +172,7 @@ int pwe_field(int field, int np, const double *x, const double *y, const double 
                                                                    P.ptr);
   SG_CUDA(cudaGetLastError());
   const int bx = (np + 31) / 32;
-  int ksplit = (2 * 152 * 2 + bx - 1) / bx;  // about four blocks of 256 threads per SM
+  int ksplit = (4 * sm_count() + bx - 1) / bx;  // about four blocks of 256 threads per SM
   const int maxs = nk / kNfWarps > 0 ? nk / kNfWarps : 1;  // keep >= one kappa node per warp
   ksplit = ksplit < 1 ? 1 : (ksplit > maxs ? maxs : ksplit);
   partial.reserve((size_t)ksplit * 3 * np);

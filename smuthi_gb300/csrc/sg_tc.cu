@@ -131,8 +131,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
   float2 *ph = reinterpret_cast<float2 *>(Xs + 4 * XTILE);    // [2 bufs][2 receivers][33] e^{i d phi}
   int *pk = reinterpret_cast<int *>(ph + 2 * 2 * 33);         // [2 bufs][2]
   float *pt = reinterpret_cast<float *>(pk + 4);              // [2 bufs][2]
-  uint64_t *bars = reinterpret_cast<uint64_t *>(pt + 4 + 2);  // 2 mbarriers (8-byte aligned: offsets are multiples of 8)
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2);
+  // 2 stage mbarriers and one for the final commit after a timeout (8-byte aligned: offsets are multiples of 8)
+  uint64_t *bars = reinterpret_cast<uint64_t *>(pt + 4 + 2);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 3);
   int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -144,7 +145,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
   for (int e = tid; e < 4 * ATILE; e += kTcThreads) As[e] = 0.f;
   if (tid == 0) {
     *abort_flag = 0;
-    for (int s = 0; s < 2; ++s)
+    for (int s = 0; s < 3; ++s)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[s])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -274,6 +275,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
     const int ns = issued > s ? (issued - s + 1) / 2 : 0;  // commits on stage s
     if (ns > 0 && !mbar_wait(smem_u32(&bars[s]), (uint32_t)((ns - 1) & 1))) ok = false;
   }
+  ok = __syncthreads_and(ok) != 0;  // one verdict for the whole CTA (the epilogue's loads are warp-collective)
+  if (!ok) {
+    // a drain wait ran out: MMAs of this CTA may still be running. One more commit tracks every
+    // tcgen05 operation the issuing thread started; wait for it (bounded) before the tensor memory
+    // is freed, so that no MMA writes columns that another CTA may allocate next. The output of this
+    // launch is undefined either way and the error flag is set.
+    if (tid == 0)
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&bars[2]))
+                   : "memory");
+    (void)mbar_wait(smem_u32(&bars[2]), 0u);
+    __syncthreads();
+  }
   if (!ok || *abort_flag) {
     if (tid == 0) atomicExch(a.err, 1);
   }
@@ -344,7 +358,7 @@ template <int NC, int R>
 static void tc_launch_t(const TcArgs &a, cudaStream_t st) {
   constexpr int NN = 2 * R;
   const size_t smem = (size_t)(4 * 128 * kBP + 4 * NN * kBP) * sizeof(float) + 2 * 2 * 33 * sizeof(float2) +
-                      4 * sizeof(int) + 6 * sizeof(float) + 2 * sizeof(uint64_t) + 2 * sizeof(uint32_t) + 64;
+                      4 * sizeof(int) + 6 * sizeof(float) + 3 * sizeof(uint64_t) + 2 * sizeof(uint32_t) + 64;
   static bool attr_done[64] = {};
   if (first_on_device(attr_done))
     SG_CUDA(cudaFuncSetAttribute(tc_coupling_kernel<NC, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -363,7 +377,7 @@ int launch_tc_matvec(sg_context *c, const double2 *x, double2 *y, int R, bool ma
     c->tc_err_init = true;
   }
   const size_t total = (size_t)c->n * (2 * R) * kBP;
-  tc_split_x_kernel<<<(unsigned)std::min<size_t>((total + 255) / 256, 152 * 16), 256, 0, st>>>(x, c->tc_xop.ptr, c->n,
+  tc_split_x_kernel<<<(unsigned)std::min<size_t>((total + 255) / 256, (size_t)sm_count() * 16), 256, 0, st>>>(x, c->tc_xop.ptr, c->n,
                                                                                               c->bs, R);
   SG_CUDA(cudaGetLastError());
   TcArgs a{};

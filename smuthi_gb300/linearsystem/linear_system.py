@@ -25,12 +25,23 @@ import numpy as np
 import scipy.sparse.linalg
 
 from .. import fields as flds
-from .._lib import SG_FP32, SG_FP64, Context
+from .._lib import SG_DF64, SG_FP32, SG_FP64, SG_PRECOND, Context
 from ..fields.expansions import SphericalWaveExpansion
 from ..utility import cuda as cu
 from .particlecoupling import prepare_lookup as look
 
 PRECISIONS = {'fp64': SG_FP64, 'mixed': SG_FP32}
+RESIDUALS = ('fp64', 'df64')
+
+
+def shipped_preconditioner(layer_system, blocksize):
+    """Name of the shipped learned-preconditioner weights for a layer system: those trained on the
+    sphere film between two half-spaces for three or more layers, those trained on spheres above a
+    substrate otherwise. Raises ValueError when no shipped weights fit the blocksize."""
+    from .. import learned
+    name = 'precond_c5' if layer_system.number_of_layers() >= 3 else 'precond_c2'
+    learned.load_params(name, blocksize)  # checks the parameter count against the blocksize
+    return name
 
 
 class SystemMatrix:
@@ -242,19 +253,37 @@ class LinearSystem:
     """Assemble and solve (1 - T W) b = T a with a GPU lookup (radial, or volume for particles at
     different heights).
 
-    Extra keyword ``precision``: 'fp64' (plain drop-in, default) or 'mixed'
-    (FP32 coupling operator inside FP64 iterative refinement; FP64 true
-    residuals and FP64 Arnoldi). ``restart`` and ``maxiter`` are GMRES
-    parameters with scipy's defaults (20, 10 x unknowns).
+    Extra keywords:
+
+    * ``precision``: 'fp64' (plain drop-in, default) or 'mixed' (FP32 coupling
+      operator inside FP64 iterative refinement, FP64 Arnoldi);
+    * ``residual``: arithmetic of the mixed form's true residuals, 'fp64' (default) or
+      'df64' (double-float on the FP32 pipe, FP64-grade);
+    * ``preconditioner``: None (default), 'learned' (the shipped weights for the layer
+      system, see ``shipped_preconditioner``) or the name of a weights file; mixed form
+      with a radial lookup only (flexible GMRES with the learned right preconditioner);
+    * ``initial_field`` may be a list of initial fields of one vacuum wavelength: their
+      right-hand sides are solved as one batch and every particle gets one scattered
+      field per initial field (``scattered_fields``; ``scattered_field`` is the first);
+    * ``restart`` and ``maxiter`` are GMRES parameters with scipy's defaults (20, 10 x
+      unknowns).
+
+    The plain form starts GMRES at x0 = rhs like the reference; the mixed form at x0 = 0.
     """
 
     def __init__(self, particle_list, initial_field, layer_system, k_parallel='default', solver_type='LU',
                  solver_tolerance=1e-4, store_coupling_matrix=True, coupling_matrix_lookup_resolution=None,
                  interpolator_kind='cubic', cuda_blocksize=None, periodicity=None,
                  ewald_sum_separation_parameter='default', number_of_threads_periodic='default',
-                 use_pvwf_coupling=False, pvwf_coupling_k_parallel=None, precision='fp64', restart=20, maxiter=None):
+                 use_pvwf_coupling=False, pvwf_coupling_k_parallel=None, precision='fp64', restart=20, maxiter=None,
+                 residual='fp64', preconditioner=None):
         self.particle_list = particle_list
-        self.initial_field = initial_field
+        self.initial_fields = list(initial_field) if isinstance(initial_field, (list, tuple)) else [initial_field]
+        if not self.initial_fields:
+            raise ValueError('at least one initial field is needed')
+        if len({f.vacuum_wavelength for f in self.initial_fields}) != 1:
+            raise ValueError('initial fields solved as one batch must share the vacuum wavelength')
+        self.initial_field = self.initial_fields[0]
         self.layer_system = layer_system
         self.k_parallel = k_parallel
         self.solver_type = solver_type
@@ -266,7 +295,13 @@ class LinearSystem:
         self.periodicity = periodicity
         if precision not in PRECISIONS:
             raise ValueError("precision must be 'fp64' or 'mixed'")
+        if residual not in RESIDUALS:
+            raise ValueError("residual must be 'fp64' or 'df64'")
+        if precision == 'fp64' and (residual != 'fp64' or preconditioner is not None):
+            raise ValueError("residual='df64' and a preconditioner need precision='mixed'")
         self.precision = precision
+        self.residual = residual
+        self.preconditioner = preconditioner
         self.restart = restart
         self.maxiter = maxiter
         self.solve_info = None
@@ -279,20 +314,26 @@ class LinearSystem:
         self.master_matrix = MasterMatrix(t_matrix=self.t_matrix, coupling_matrix=self.coupling_matrix)
 
     def compute_initial_field_coefficients(self):
+        """Regular SWE of every initial field at every particle (``p.initial_fields``; ``p.initial_field``
+        is the first)."""
         groups = {}
         for i, p in enumerate(self.particle_list):
             groups.setdefault((p.l_max, p.m_max, self.layer_system.layer_number(p.position[2])), []).append(i)
-        for (lm, mm, layer), idx in groups.items():
-            pos = np.array([self.particle_list[i].position for i in idx], dtype=float)
-            coef = self.initial_field.swe_coefficients(pos, self.layer_system, lm, mm)
-            k = self.initial_field.angular_frequency() * self.layer_system.refractive_indices[layer]
-            for row, i in enumerate(idx):
-                p = self.particle_list[i]
-                swe = SphericalWaveExpansion(k=k, l_max=lm, m_max=mm, kind='regular', reference_point=p.position,
-                                             lower_z=self.layer_system.lower_zlimit(layer),
-                                             upper_z=self.layer_system.upper_zlimit(layer))
-                swe.coefficients = coef[row]
-                p.initial_field = swe
+            p.initial_fields = [None] * len(self.initial_fields)
+        for q, field in enumerate(self.initial_fields):
+            for (lm, mm, layer), idx in groups.items():
+                pos = np.array([self.particle_list[i].position for i in idx], dtype=float)
+                coef = field.swe_coefficients(pos, self.layer_system, lm, mm)
+                k = field.angular_frequency() * self.layer_system.refractive_indices[layer]
+                for row, i in enumerate(idx):
+                    p = self.particle_list[i]
+                    swe = SphericalWaveExpansion(k=k, l_max=lm, m_max=mm, kind='regular', reference_point=p.position,
+                                                 lower_z=self.layer_system.lower_zlimit(layer),
+                                                 upper_z=self.layer_system.upper_zlimit(layer))
+                    swe.coefficients = coef[row]
+                    p.initial_fields[q] = swe
+        for p in self.particle_list:
+            p.initial_field = p.initial_fields[0]
 
     def compute_t_matrix(self):
         for p in self.particle_list:
@@ -340,25 +381,61 @@ class LinearSystem:
             st = self.solver_type.lower()
             if st != 'gmres':
                 raise NotImplementedError('solver_type %r is not provided (gmres only)' % self.solver_type)
-            rhs = self.t_matrix.right_hand_side()
+            cols = []
+            for q in range(len(self.initial_fields)):
+                for p in self.particle_list:
+                    p.initial_field = p.initial_fields[q]
+                cols.append(self.t_matrix.right_hand_side())
+            for p in self.particle_list:
+                p.initial_field = p.initial_fields[0]
+            nrhs = len(cols)
+            rhs = cols[0] if nrhs == 1 else np.ascontiguousarray(np.stack(cols, axis=1))
             start = time.time()
             ctx = self.coupling_matrix.context
-            b, info = ctx.gmres(rhs, rhs, self.solver_tolerance, restart=self.restart, maxiter=self.maxiter or 0,
-                                precision=PRECISIONS[self.precision], raise_on_failure=False)
-            if info.converged < 1:
+            flags = PRECISIONS[self.precision]
+            if self.precision == 'mixed':
+                if self.residual == 'df64':
+                    flags |= SG_DF64
+                if self.preconditioner is not None:
+                    self._attach_preconditioner(ctx)
+                    flags |= SG_PRECOND
+            x0 = rhs if self.precision == 'fp64' else np.zeros_like(rhs)
+            b, info = ctx.gmres(rhs, x0, self.solver_tolerance, restart=self.restart, maxiter=self.maxiter or 0,
+                                precision=flags, raise_on_failure=False)
+            if info.converged < nrhs:
                 # the reference ignores GMRES's info flag (linear_system.py:285); report it instead
                 warnings.warn('GMRES did not reach the tolerance (rel. residual %.2e)' % info.max_rel_residual)
             self.solve_info = info.as_dict()
             sys.stdout.write('Solve (GMRES)             : Iter %d | Rel. residual: %.2e | elapsed: %ds\n'
                              % (info.iterations, info.max_rel_residual, int(time.time() - start)))
+            B = b.reshape(-1, 1) if b.ndim == 1 else b
+        else:
+            B = np.zeros((0, len(self.initial_fields)), complex)
         for i, p in enumerate(self.particle_list):
             layer = self.layer_system.layer_number(p.position[2])
             k = flds.angular_frequency(self.initial_field.vacuum_wavelength) * self.layer_system.refractive_indices[
                 layer]
-            p.scattered_field = SphericalWaveExpansion(k=k, l_max=p.l_max, m_max=p.m_max, kind='outgoing',
-                                                       reference_point=p.position,
-                                                       lower_z=self.layer_system.lower_zlimit(layer),
-                                                       upper_z=self.layer_system.upper_zlimit(layer))
-            p.scattered_field.coefficients = b[self.master_matrix.index_block(i)]
-            p.scattered_field.validity_conditions.append(p.is_outside)
-            self.initial_field.validity_conditions.append(p.is_outside)
+            p.scattered_fields = []
+            for q in range(len(self.initial_fields)):
+                swe = SphericalWaveExpansion(k=k, l_max=p.l_max, m_max=p.m_max, kind='outgoing',
+                                             reference_point=p.position, lower_z=self.layer_system.lower_zlimit(layer),
+                                             upper_z=self.layer_system.upper_zlimit(layer))
+                swe.coefficients = B[self.master_matrix.index_block(i), q]
+                swe.validity_conditions.append(p.is_outside)
+                p.scattered_fields.append(swe)
+            p.scattered_field = p.scattered_fields[0]
+            for field in self.initial_fields:
+                field.validity_conditions.append(p.is_outside)
+
+    def _attach_preconditioner(self, ctx):
+        """Select the learned preconditioner on the context (radial lookup, uniform particles)."""
+        from .. import learned
+        cm = self.coupling_matrix
+        if not isinstance(cm, CouplingMatrixRadialLookupCUDA):
+            raise NotImplementedError('the learned preconditioner serves the radial lookup only')
+        bs = cm.blocksize
+        name = shipped_preconditioner(self.layer_system, bs) if self.preconditioner == 'learned' \
+            else self.preconditioner
+        xy = np.array([p.position[:2] for p in self.particle_list], dtype=float)
+        learned.attach(ctx, xy, bs, learned.load_params(name, bs), k=learned.load_meta(name)['k'])
+        self.preconditioner_name = name

@@ -1,8 +1,21 @@
 """Simulation driver mirroring smuthi/simulation.py (:92-153 constructor, :363-414 run).
 
-Same keyword arguments as the reference; the extra ``precision`` keyword
-selects the plain FP64 drop-in ('fp64') or the mixed-precision form
-('mixed'). ``run`` returns (preparation, solution, post-processing) seconds.
+Same keyword arguments as the reference. Extra keywords select the solve form:
+
+* ``precision``: the plain FP64 drop-in ('fp64', default) or the mixed-precision form ('mixed':
+  FP32 coupling operator inside FP64 iterative refinement);
+* ``residual``: the mixed form's true residuals in FP64 ('fp64', default) or in FP64-grade
+  double-float arithmetic on the FP32 pipe ('df64');
+* ``preconditioner``: None, 'learned' (the shipped learned right preconditioner for the layer
+  system) or a weights-file name;
+* ``initial_field`` may be a list of plane waves of one wavelength, solved as one batch: after
+  ``run`` every particle holds ``scattered_fields`` (one per wave) and ``select_wave(q)`` makes wave
+  q the simulation's ``initial_field`` and each particle's ``scattered_field`` (what the
+  post-processing functions read).
+
+The chosen form of this package is ``precision='mixed', residual='df64',
+preconditioner='learned'`` with several plane waves. ``run`` returns (preparation, solution,
+post-processing) seconds.
 """
 import sys
 import time
@@ -25,10 +38,11 @@ class Simulation:
                  check_circumscribing_spheres=True, do_sanity_check=True, periodicity=None,
                  ewald_sum_separation_parameter='default', number_of_threads_periodic='default',
                  use_pvwf_coupling=False, pvwf_coupling_neff_max=None, pvwf_coupling_neff_resolution=1e-2,
-                 precision='fp64', restart=20, maxiter=None):
+                 precision='fp64', restart=20, maxiter=None, residual='fp64', preconditioner=None):
         self.layer_system = layer_system
         self.particle_list = particle_list
-        self.initial_field = initial_field
+        self.initial_fields = list(initial_field) if isinstance(initial_field, (list, tuple)) else [initial_field]
+        self.initial_field = self.initial_fields[0]
         self.k_parallel = k_parallel
         self.angular_resolution = angular_resolution
         self.neff_waypoints = neff_waypoints
@@ -51,6 +65,8 @@ class Simulation:
         if use_pvwf_coupling:
             raise NotImplementedError('plane-wave coupling is not part of the radial-lookup path')
         self.precision = precision
+        self.residual = residual
+        self.preconditioner = preconditioner
         self.restart = restart
         self.maxiter = maxiter
         self.post_processing = None
@@ -115,14 +131,27 @@ class Simulation:
     def set_default_angles(self):
         flds.default_azimuthal_angles, flds.default_polar_angles = flds.angular_arrays(self.angular_resolution)
 
+    def select_wave(self, q):
+        """Make initial field q (of a batch) the simulation's ``initial_field`` and every particle's
+        ``initial_field`` and ``scattered_field`` that of wave q (the post-processing reads these)."""
+        self.initial_field = self.initial_fields[q]
+        for p in self.particle_list:
+            if getattr(p, 'initial_fields', None):
+                p.initial_field = p.initial_fields[q]
+            if getattr(p, 'scattered_fields', None):
+                p.scattered_field = p.scattered_fields[q]
+
     def initialize_linear_system(self):
         self.linear_system = lsys.LinearSystem(
-            particle_list=self.particle_list, initial_field=self.initial_field, layer_system=self.layer_system,
+            particle_list=self.particle_list,
+            initial_field=self.initial_fields if len(self.initial_fields) > 1 else self.initial_field,
+            layer_system=self.layer_system,
             k_parallel=self.k_parallel, solver_type=self.solver_type, solver_tolerance=self.solver_tolerance,
             store_coupling_matrix=self.store_coupling_matrix,
             coupling_matrix_lookup_resolution=self.coupling_matrix_lookup_resolution,
             interpolator_kind=self.coupling_matrix_interpolator_kind, periodicity=self.periodicity,
-            precision=self.precision, restart=self.restart, maxiter=self.maxiter)
+            precision=self.precision, restart=self.restart, maxiter=self.maxiter, residual=self.residual,
+            preconditioner=self.preconditioner)
 
     def run(self):
         """Prepare and solve; returns (preparation_time, solution_time, postprocessing_time)."""

@@ -318,3 +318,57 @@ def test_one_and_two_particle_systems(count, gpu_context):
         sol, info = gpu_context.gmres(b, np.zeros_like(b), tol, precision=prec)
         assert info.converged == 1
         assert gpu_context.true_residual(b, sol)[0] <= tol
+
+
+def test_simulation_chosen_form_two_waves(gpu_context):
+    """The chosen form through the reference-shaped API: two plane waves solved as one batch with the
+    mixed-precision operator, double-float residuals and the learned preconditioner. At a relative
+    residual of 1e-6 both cross sections of each wave are within 1e-6 of the reference's; solved to
+    1e-10 both solutions are within 1e-6 of the reference's."""
+    from smuthi_gb300 import initial_field as init, layers, particles, simulation
+    from smuthi_gb300.postprocessing import far_field as ff
+    g = gc.load("c5s")
+    ls = layers.LayerSystem([float(x) for x in g["thicknesses"]], [float(complex(x).real) for x in g["layer_n"]])
+    waves = [gc.plane_wave(g, q, init.PlaneWave) for q in range(2)]
+    for tol in (1e-6, 1e-10):
+        parts = [particles.Sphere(position=list(p), refractive_index=complex(n), radius=float(r), l_max=int(lm),
+                                  m_max=int(mm))
+                 for p, n, r, lm, mm in zip(g["positions"], g["n_particle"], g["radii"], g["l_max"], g["m_max"])]
+        sim = simulation.Simulation(layer_system=ls, particle_list=parts, initial_field=waves, solver_type='gmres',
+                                    solver_tolerance=tol, store_coupling_matrix=False,
+                                    coupling_matrix_lookup_resolution=float(g["resolution"]),
+                                    coupling_matrix_interpolator_kind='linear', log_to_terminal=False,
+                                    precision='mixed', residual='df64', preconditioner='learned', restart=32)
+        sim.run()
+        info = sim.linear_system.solve_info
+        assert info["converged"] == 2 and info["max_rel_residual"] <= tol
+        assert sim.linear_system.preconditioner_name == "precond_c5"
+        for q in range(2):
+            sim.select_wave(q)
+            b = np.concatenate([p.scattered_field.coefficients for p in parts])
+            if tol == 1e-10:
+                assert gc.relerr(b, g["b_linear_w%d" % q]) < 1e-6
+            else:
+                for fn, key in ((ff.extinction_cross_section, "sigma_ext"), (ff.total_scattering_cross_section,
+                                                                              "sigma_sca")):
+                    ref = g["%s_linear_w%d" % (key, q)]
+                    assert abs(fn(sim) - ref) <= 1e-6 * abs(ref), (key, q)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_not_converged_returns_last_iterate(precision, gpu_context):
+    """An iteration limit below what the tolerance needs: SG_ERR_NOT_CONVERGED (NotConverged), and
+    without raising, the last iterate (its FP64-true residual below the start's) and converged = 0."""
+    from smuthi_gb300 import _lib
+    g = gc.load("c1")
+    _product_system(g, "linear", gpu_context)
+    rhs = g["rhs_linear_w0"]
+    prec = _lib.SG_FP64 if precision == "fp64" else _lib.SG_FP32 | _lib.SG_DF64
+    with pytest.raises(_lib.NotConverged) as e:
+        gpu_context.gmres(rhs, rhs, 1e-13, restart=5, maxiter=3, precision=prec)
+    assert e.value.code == _lib.SG_ERR_NOT_CONVERGED
+    x, info = gpu_context.gmres(rhs, np.zeros_like(rhs), 1e-13, restart=5, maxiter=3, precision=prec,
+                                raise_on_failure=False)
+    assert info.converged == 0
+    r = float(gpu_context.true_residual(rhs, x)[0])
+    assert 1e-13 < r < 1.0 and info.max_rel_residual > 1e-13
