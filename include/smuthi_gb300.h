@@ -219,6 +219,17 @@ int sg_coupling_matvec_linear_noalloc(int device, int n_particles, const void *x
 int sg_bessel_jac_table(sg_context *ctx, const void *kappa, const void *jac, int nk, const void *rho, int nr,
                         int nmax, void *out, void *stream);
 
+/* Sommerfeld contraction of the layer-mediated lookup table on the GPU (the reference's GPU helper
+ * smuthi/linearsystem/particlecoupling/prepare_lookup_cuda.py:55-95, driven at prepare_lookup.py:439-456,
+ * integrates each (n1, n2) column over the contour per radial point):
+ * out[r * out_stride + cols[j]] = (factor_re + i factor_im) * sum_k a[r][k] * g[k][j] for r < nr,
+ * j < ncols. a: complex128[nr][nk] (one order of sg_bessel_jac_table's output), g: complex128[nk][ncols]
+ * (integrand times trapezoid weights of the columns of one |m1 - m2|), cols: int32[ncols] output
+ * columns, out: complex128 rows of out_stride; all device buffers on the context's device. FP64
+ * throughout, the k sum in order. Asynchronous on `stream` (NULL = context stream). */
+int sg_lookup_contract(sg_context *ctx, const void *a, int nr, int nk, const void *g, int ncols, const int *cols,
+                       double factor_re, double factor_im, void *out, long long out_stride, void *stream);
+
 /* Particle sum of the scattered field's plane-wave expansion for the cross sections (the reference
  * converts each particle's expansion on the host: smuthi/postprocessing/far_field.py:363-427,
  * smuthi/postprocessing/scattered_field.py:80-150, smuthi/fields/transformations.py:133-233):

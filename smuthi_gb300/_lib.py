@@ -31,6 +31,7 @@ EXPORTS = ("sg_last_error", "sg_version", "sg_create", "sg_destroy", "sg_set_par
            "sg_coupling_matvec_linear_noalloc", "sg_precond_param_count", "sg_precond_add_graph",
            "sg_precond_select", "sg_precond_clear", "sg_precond_set_params", "sg_precond_get_params",
            "sg_precond_apply_dev", "sg_precond_train_step", "sg_precond_export_blocks", "sg_bessel_jac_table",
+           "sg_lookup_contract",
            "sg_farfield_sum", "sg_set_volume_lookup", "sg_farfield_sum_heights", "sg_pwe_field")
 
 
@@ -91,6 +92,7 @@ def _declare(L):
         "sg_fp32_set_kernel": [_P, _I, _I, _I],
         "sg_coupling_matvec_linear_noalloc": [_I, _I, _P, _I, _P, _I, _D, _D, _P, _P, _P, _I, _P],
         "sg_bessel_jac_table": [_P, _P, _P, _I, _P, _I, _I, _P, _P],
+        "sg_lookup_contract": [_P, _P, _I, _I, _P, _I, _P, _D, _D, _P, ctypes.c_longlong, _P],
         "sg_farfield_sum": [_P, _I, _P, _I, _I, _P, _I, _P, _I, _P, _P, _I, _P, _P, _P],
         "sg_farfield_sum_heights": [_P, _I, _P, _I, _I, _P, _I, _P, _I, _P, _P, _I, _P, _P, _P, _P],
         "sg_pwe_field": [_P, _I, _I, _P, _P, _P, _I, _P, _P, _I, _P, _P, _D, _D, _D, _P, _P],
@@ -316,6 +318,13 @@ class Context:
         check(lib().sg_bessel_jac_table(self.h, ctypes.c_void_p(kappa_ptr), ctypes.c_void_p(jac_ptr), int(nk),
                                         ctypes.c_void_p(rho_ptr), int(nr), int(nmax), ctypes.c_void_p(out_ptr),
                                         ctypes.c_void_p(stream or 0)))
+
+    def lookup_contract_dev(self, a_ptr, nr, nk, g_ptr, ncols, cols_ptr, factor, out_ptr, out_stride, stream=None):
+        """out[r * out_stride + cols[j]] = factor * sum_k a[r][k] g[k][j] on the device (see the header)."""
+        check(lib().sg_lookup_contract(self.h, ctypes.c_void_p(a_ptr), int(nr), int(nk), ctypes.c_void_p(g_ptr),
+                                       int(ncols), ctypes.c_void_p(cols_ptr), float(complex(factor).real),
+                                       float(complex(factor).imag), ctypes.c_void_p(out_ptr), int(out_stride),
+                                       ctypes.c_void_p(stream or 0)))
 
     def pwe_field_dev(self, field, n, x_ptr, y_ptr, z_ptr, nk, kpar_ptr, kz_ptr, na, alpha_ptr, g_ptr, k, omega,
                       out_ptr, stream=None):

@@ -654,6 +654,19 @@ int sg_bessel_jac_table(sg_context *ctx, const void *kappa, const void *jac, int
   });
 }
 
+int sg_lookup_contract(sg_context *ctx, const void *a, int nr, int nk, const void *g, int ncols, const int *cols,
+                       double factor_re, double factor_im, void *out, long long out_stride, void *stream) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx && a && g && cols && out, "null argument");
+    use_device(ctx);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    sg::lookup_contract((const double2 *)a, nr, nk, (const double2 *)g, ncols, cols,
+                        make_double2(factor_re, factor_im), (double2 *)out, out_stride, st);
+    ctx->launches += 1;
+    return SG_OK;
+  });
+}
+
 int sg_farfield_sum_heights(sg_context *ctx, int n_particles, const void *xy, int blocksize, int nrhs,
                             const void *coef, int m_max, const int32_t *m_of_n, int nk, const void *kpar,
                             const void *S, int na, const void *alpha, const void *zphase, void *out, void *stream) {

@@ -168,6 +168,9 @@ int pwe_field(int field, int np, const double *x, const double *y, const double 
 // Bessel factors of the layer-mediated lookup table (sg_table.cu)
 void bessel_jac_table(const double2 *kp, const double2 *jac, int nk, const double *rho, int nr, int nmax,
                       double2 *out, cudaStream_t st);
+// out[r * out_stride + cols[j]] = factor * sum_k a[r][k] g[k][j] (FP64 tiled complex GEMM, sg_table.cu)
+void lookup_contract(const double2 *a, int nr, int nk, const double2 *g, int ncols, const int *cols, double2 factor,
+                     double2 *out, long long out_stride, cudaStream_t st);
 
 // particle sum of the scattered plane-wave expansion (sg_farfield.cu); synchronous
 void farfield_sum(const double2 *xy, int n, int bs, int nrhs, const double2 *coef, int mmax, const int *mofn_host,

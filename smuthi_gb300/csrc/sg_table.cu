@@ -149,6 +149,79 @@ __global__ void bessel_jac_kernel(const double2 *kp, const double2 *jac, int nk,
   }
 }
 
+// ------------------------------------------------------------------ Sommerfeld contraction
+// out[r * out_stride + cols[j]] = factor * sum_k a[r][k] g[k][j]: the layer-mediated table's trapezoid
+// over the contour for the columns (n1, n2) of one |m1 - m2|, a = J_|dm|(kappa_k rho_r) jac_k (the
+// Bessel factors, resident on the device), g[k][j] the per-column integrand times the trapezoid
+// weights. A tiled FP64 complex GEMM: 64 rows x 32 columns per block of 256 threads, each thread
+// 4 x 2 outputs, K in steps of 16 through shared memory; the sum over k runs in order on the FP64 pipe.
+static constexpr int kCtTM = 64, kCtTN = 32, kCtTK = 16;
+
+__global__ void __launch_bounds__(256) contract_kernel(const double2 *__restrict__ a, int nr, int nk,
+                                                       const double2 *__restrict__ g, int ncols,
+                                                       const int *__restrict__ cols, double2 factor,
+                                                       double2 *__restrict__ out, long long out_stride) {
+  __shared__ double2 As[kCtTM][kCtTK + 1];
+  __shared__ double2 Bs[kCtTK][kCtTN];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // 16 x 16 threads
+  const int r0 = blockIdx.y * kCtTM, c0 = blockIdx.x * kCtTN;
+  double2 acc[4][2];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) acc[u][v] = make_double2(0.0, 0.0);
+  for (int k0 = 0; k0 < nk; k0 += kCtTK) {
+    for (int e = threadIdx.x; e < kCtTM * kCtTK; e += 256) {
+      const int rr = e / kCtTK, kk = e - rr * kCtTK;
+      const int r = r0 + rr, k = k0 + kk;
+      As[rr][kk] = (r < nr && k < nk) ? a[(size_t)r * nk + k] : make_double2(0.0, 0.0);
+    }
+    for (int e = threadIdx.x; e < kCtTK * kCtTN; e += 256) {
+      const int kk = e / kCtTN, cc = e - kk * kCtTN;
+      const int k = k0 + kk, c = c0 + cc;
+      Bs[kk][cc] = (k < nk && c < ncols) ? g[(size_t)k * ncols + c] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < kCtTK; ++kk) {
+      double2 av[4], bv[2];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) av[u] = As[ty + 16 * u][kk];
+#pragma unroll
+      for (int v = 0; v < 2; ++v) bv[v] = Bs[kk][tx + 16 * v];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+          acc[u][v].x = fma(av[u].x, bv[v].x, fma(-av[u].y, bv[v].y, acc[u][v].x));
+          acc[u][v].y = fma(av[u].x, bv[v].y, fma(av[u].y, bv[v].x, acc[u][v].y));
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int r = r0 + ty + 16 * u, c = c0 + tx + 16 * v;
+      if (r < nr && c < ncols) {
+        const double2 s = acc[u][v];
+        out[(size_t)r * out_stride + cols[c]] =
+            make_double2(factor.x * s.x - factor.y * s.y, factor.x * s.y + factor.y * s.x);
+      }
+    }
+}
+
+void lookup_contract(const double2 *a, int nr, int nk, const double2 *g, int ncols, const int *cols, double2 factor,
+                     double2 *out, long long out_stride, cudaStream_t st) {
+  SG_REQUIRE(nr >= 1 && nk >= 1 && ncols >= 1, "empty contraction");
+  SG_REQUIRE(out_stride >= 1, "bad output row stride");
+  dim3 grid((ncols + kCtTN - 1) / kCtTN, (nr + kCtTM - 1) / kCtTM);
+  SG_REQUIRE(grid.y <= 65535, "too many radial points for one contraction launch");
+  contract_kernel<<<grid, 256, 0, st>>>(a, nr, nk, g, ncols, cols, factor, out, out_stride);
+  SG_CUDA(cudaGetLastError());
+}
+
 void bessel_jac_table(const double2 *kp, const double2 *jac, int nk, const double *rho, int nr, int nmax,
                       double2 *out, cudaStream_t st) {
   SG_REQUIRE(nk >= 1 && nr >= 1, "empty contour or radial grid");

@@ -98,10 +98,11 @@ def direct_part(k_is, rho, l_max, m_max, rho_min_pair):
 def layer_mediated_part(vacuum_wavelength, layer_system, i_s, dz, rho, k_parallel, l_max, m_max, context=None):
     """Layer-mediated coupling table (complex128) [len_rho, B, B].
 
-    With a library ``context`` the Bessel factors J_|dm|(kappa rho) * jac (the dominant cost of the
-    build) are evaluated on that context's GPU by ``sg_bessel_jac_table``; without one on the host with
-    scipy, as the reference does. The contraction with the per-(n1, n2) integrand is a small FP64 GEMM
-    on the host in both cases (a library FP64 GEMM on the device may use reduced-precision emulation).
+    With a library ``context`` the Bessel factors J_|dm|(kappa rho) * jac are evaluated on that
+    context's GPU by ``sg_bessel_jac_table`` and stay there, and the contour sum with the per-(n1, n2)
+    integrand runs on the same GPU in the library's own FP64 contraction kernel
+    (``sg_lookup_contract``); only the small integrand (B^2 x len(kappa)) is formed on the host.
+    Without a context both run on the host with scipy and numpy, as the reference does.
     """
     k_is = layer_system.wavenumber(i_s, vacuum_wavelength)
     omega = flds.angular_frequency(vacuum_wavelength)
@@ -132,20 +133,18 @@ def layer_mediated_part(vacuum_wavelength, layer_system, i_s, dz, rho, k_paralle
     wts[:-1] += dkp
     wts[1:] += dkp
     jac = kp / (kz * k_is)
-    wr = np.zeros((len(rho), bs * bs), complex)
     dmat = np.abs(mm[:, None] - mm[None, :])
-    besjac_host = _bessel_factors(kp, jac, rho, 2 * m_max, context)
+    if context is not None:
+        return _layer_mediated_contract_device(kp, jac, rho, X, Bn, wts, dmat, m_max, bs, context)
+    wr = np.zeros((len(rho), bs * bs), complex)
     for dm in range(2 * m_max + 1):
         n1s, n2s = np.nonzero(dmat == dm)
         if len(n1s) == 0:
             continue
         belbe = np.einsum('pcak,pcak->ak', X[:, :, n1s, :], Bn[:, :, n2s, :])  # [pairs, k]
         G = (belbe * wts[None, :]).T  # [k, pairs]
-        if besjac_host is not None:
-            wr[:, n1s * bs + n2s] = 2 * ipow(dm) * (besjac_host[dm] @ G)
-        else:
-            besjac = scipy.special.jv(dm, kp[None, :] * rho[:, None]) * jac[None, :]
-            wr[:, n1s * bs + n2s] = 2 * ipow(dm) * (besjac @ G)
+        besjac = scipy.special.jv(dm, kp[None, :] * rho[:, None]) * jac[None, :]
+        wr[:, n1s * bs + n2s] = 2 * ipow(dm) * (besjac @ G)
     return wr.reshape(len(rho), bs, bs)
 
 
@@ -297,7 +296,29 @@ def layer_mediated_volume(vacuum_wavelength, layer_system, i_s, rho, sz, dz, k_p
     return wr_pl.reshape(nr, nz, bs, bs), wr_mn.reshape(nr, nz, bs, bs)
 
 
-def _bessel_factors(kp, jac, rho, nmax, context):
+def _layer_mediated_contract_device(kp, jac, rho, X, Bn, wts, dmat, m_max, bs, context):
+    """Layer-mediated table [len_rho, B, B] with the Bessel factors and the contour sum on the GPU."""
+    import torch
+    dev = torch.device("cuda", context.device)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    besjac = _bessel_factors(kp, jac, rho, 2 * m_max, context, keep_on_device=True)
+    nr, nk = len(rho), len(kp)
+    out = torch.zeros((nr, bs * bs), dtype=torch.complex128, device=dev)
+    keep = []  # the integrand uploads live until the stream has run the contractions
+    for dm in range(2 * m_max + 1):
+        n1s, n2s = np.nonzero(dmat == dm)
+        if len(n1s) == 0:
+            continue
+        belbe = np.einsum('pcak,pcak->ak', X[:, :, n1s, :], Bn[:, :, n2s, :])  # [pairs, k]
+        g = torch.from_numpy(np.ascontiguousarray((belbe * wts[None, :]).T)).to(dev)  # [k, pairs]
+        cols = torch.from_numpy((n1s * bs + n2s).astype(np.int32)).to(dev)
+        keep += [g, cols]
+        context.lookup_contract_dev(besjac[dm].data_ptr(), nr, nk, g.data_ptr(), len(n1s), cols.data_ptr(),
+                                    2 * ipow(dm), out.data_ptr(), bs * bs, stream=stream)
+    return out.cpu().numpy().reshape(nr, bs, bs)
+
+
+def _bessel_factors(kp, jac, rho, nmax, context, keep_on_device=False):
     """J_n(kappa rho) * jac for n = 0..nmax on the context's GPU ([n, rho, kappa]); None without one."""
     if context is None:
         return None
@@ -310,7 +331,7 @@ def _bessel_factors(kp, jac, rho, nmax, context):
     out = torch.empty((nmax + 1, len(rho), len(kp)), dtype=torch.complex128, device=dev)
     context.bessel_jac_table_dev(kp_d.data_ptr(), jac_d.data_ptr(), len(kp), rho_d.data_ptr(), len(rho), nmax,
                                  out.data_ptr(), stream=stream)
-    return out.cpu().numpy()
+    return out if keep_on_device else out.cpu().numpy()
 
 
 def volumetric_coupling_lookup_table(vacuum_wavelength, particle_list, layer_system, k_parallel='default',

@@ -76,3 +76,30 @@ def test_bessel_argument_checks(gpu_context):
         gpu_context.bessel_jac_table_dev(8, 8, 1, 8, 1, 33, 8)  # order beyond the kernel's table
     with pytest.raises(_lib.SmuthiGB300Error):
         gpu_context.bessel_jac_table_dev(8, 8, 0, 8, 1, 4, 8)  # empty contour
+
+
+def test_contraction_kernel_matches_numpy(gpu_context):
+    """sg_lookup_contract on ragged sizes (rows, contour points and columns not multiples of its tiles)
+    with scattered output columns, against numpy in FP64; columns not listed stay untouched."""
+    import torch
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(4)
+    nr, nk, nc, stride = 131, 37, 45, 60
+    a = rng.standard_normal((nr, nk)) + 1j * rng.standard_normal((nr, nk))
+    g = rng.standard_normal((nk, nc)) + 1j * rng.standard_normal((nk, nc))
+    cols = rng.permutation(stride)[:nc].astype(np.int32)
+    fac = 2 * 1j ** 3
+    out = np.full((nr, stride), 7.0 + 0j)
+    a_d, g_d, c_d = (torch.from_numpy(np.ascontiguousarray(v)).to(dev) for v in (a, g, cols))
+    o_d = torch.from_numpy(out.copy()).to(dev)
+    gpu_context.lookup_contract_dev(a_d.data_ptr(), nr, nk, g_d.data_ptr(), nc, c_d.data_ptr(), fac, o_d.data_ptr(),
+                                    stride)
+    torch.cuda.synchronize(dev)
+    got = o_d.cpu().numpy()
+    ref = out.copy()
+    ref[:, cols] = fac * (a @ g)
+    assert gc.relerr(got, ref) < 1e-14
+    from smuthi_gb300 import _lib
+    with pytest.raises(_lib.SmuthiGB300Error):
+        gpu_context.lookup_contract_dev(a_d.data_ptr(), nr, nk, g_d.data_ptr(), 0, c_d.data_ptr(), fac,
+                                        o_d.data_ptr(), stride)
