@@ -447,7 +447,7 @@ static int solve_dev_impl(sg_context *ctx, const double2 *b, double2 *x, int nrh
              "a volume lookup supports SG_FP64 and SG_FP32 (| SG_BLOCK_GMRES) solves only");
   if (precision & SG_PRECOND) {
     SG_REQUIRE(ctx->p_active >= 0, "SG_PRECOND needs a preconditioner graph (sg_precond_select)");
-    SG_REQUIRE(ctx->p_count == sg::precond_param_count(ctx->bs), "SG_PRECOND needs parameters (sg_precond_set_params)");
+    SG_REQUIRE(ctx->p_layers > 0 && ctx->p_bs == ctx->bs, "SG_PRECOND needs parameters (sg_precond_set_params)");
     SG_REQUIRE(nrhs <= 64, "SG_PRECOND handles at most 64 right-hand sides per solve");
   }
   use_device(ctx);

@@ -178,7 +178,8 @@ void farfield_sum(const double2 *xy, int n, int bs, int nrhs, const double2 *coe
                   double2 *out, cudaStream_t st);
 
 // ---------------------------------------------------------------- learned preconditioner (sg_precond.cu)
-int precond_param_count(int bs);
+int precond_param_count(int bs);   // the default (3-layer) network
+int precond_layers(int bs, int count);  // depth of a parameter vector (0: no valid depth)
 void precond_add_graph(sg_context *c, int k, const int *nbr_host, int *graph_id, cudaStream_t st);
 void precond_set_params(sg_context *c, int bs, const float *params, int count, cudaStream_t st);
 void precond_get_params(sg_context *c, float *params, int count, cudaStream_t st);
@@ -273,7 +274,7 @@ struct sg_context {
     sg::DevBuf<float2> G;       // [n][k1][bs][bs], n2 fastest
   };
   std::vector<std::unique_ptr<PGraph>> pgraphs;
-  int p_active = -1, p_bs = 0, p_count = 0;
+  int p_active = -1, p_bs = 0, p_count = 0, p_layers = 0;
   sg::DevBuf<float> p_w, p_g, p_m, p_v;  // FP32 master weights, gradient, Adam moments
   sg::DevBuf<__nv_bfloat16> p_wb;        // BF16 copy used by the forward and backward kernels
   sg::DevBuf<float> p_act, p_back;       // activations, backward scratch

@@ -29,11 +29,21 @@
 namespace sg {
 
 static constexpr int kHid = 128;
-static constexpr int kLayers = 3;
+static constexpr int kLayers = 3;     // the default network depth (sg_precond_param_count)
+static constexpr int kMaxLayers = 8;  // deeper networks: the parameter count sets the depth
 
-int precond_param_count(int bs) {
+static int per_layer_count(int bs) {
   const int F = 4 * bs, O = 2 * bs;
-  return kLayers * (kHid * F + kHid + O * kHid + O + 2);
+  return kHid * F + kHid + O * kHid + O + 2;
+}
+
+int precond_param_count(int bs) { return kLayers * per_layer_count(bs); }
+
+// layers of a parameter vector of `count` floats (0 when the count fits no depth 1..kMaxLayers)
+int precond_layers(int bs, int count) {
+  const int per = per_layer_count(bs);
+  if (count <= 0 || count % per != 0 || count / per > kMaxLayers) return 0;
+  return count / per;
 }
 
 struct LayerOff {
@@ -474,8 +484,8 @@ void precond_add_graph(sg_context *c, int k, const int *nbr_host, int *graph_id,
 }
 
 void precond_set_params(sg_context *c, int bs, const float *params, int count, cudaStream_t st) {
-  SG_REQUIRE(bs >= 1 && bs <= 64 && count == precond_param_count(bs),
-             "parameter count does not match the network for this blocksize");
+  SG_REQUIRE(bs >= 1 && bs <= 64 && precond_layers(bs, count) > 0,
+             "parameter count does not match a network of 1..8 layers for this blocksize");
   c->p_w.reserve(count);
   c->p_wb.reserve(count);
   c->p_g.reserve(count);
@@ -489,12 +499,13 @@ void precond_set_params(sg_context *c, int bs, const float *params, int count, c
   SG_CUDA(cudaStreamSynchronize(st));
   c->p_bs = bs;
   c->p_count = count;
+  c->p_layers = precond_layers(bs, count);
   c->launches += 1;
 }
 
 struct Fwd {
-  float2 *u, *a[kLayers], *h[kLayers + 1];
-  float *p[kLayers];
+  float2 *u, *a[kMaxLayers], *h[kMaxLayers + 1];
+  float *p[kMaxLayers];
   float *sq;
 };
 
@@ -502,24 +513,24 @@ struct Fwd {
 // activations the backward pass needs.
 static void forward(sg_context *c, const sg_context::PGraph &g, const double2 *v, int S, Fwd &f, cudaStream_t st) {
   SG_REQUIRE(S >= 1 && S <= 64, "the preconditioner handles 1..64 vectors per call");
-  SG_REQUIRE(c->p_count == precond_param_count(g.bs) && c->p_bs == g.bs,
-             "preconditioner parameters are not set for this blocksize");
+  SG_REQUIRE(c->p_layers > 0 && c->p_bs == g.bs, "preconditioner parameters are not set for this blocksize");
+  const int nl = c->p_layers;
   const int n = g.n, bs = g.bs;
   const size_t len = (size_t)n * bs * S, rows = (size_t)n * S;
-  c->p_act.reserve(len * 2 * (2 * kLayers + 2) + rows * kHid * kLayers + 64);
+  c->p_act.reserve(len * 2 * (2 * nl + 2) + rows * kHid * nl + 64);
   float *base = c->p_act.ptr;
   size_t off = 0;
   f.u = reinterpret_cast<float2 *>(base + off);
   off += len * 2;
-  for (int l = 0; l < kLayers; ++l) {
+  for (int l = 0; l < nl; ++l) {
     f.a[l] = reinterpret_cast<float2 *>(base + off);
     off += len * 2;
   }
-  for (int l = 0; l <= kLayers; ++l) {
+  for (int l = 0; l <= nl; ++l) {
     f.h[l] = reinterpret_cast<float2 *>(base + off);
     off += len * 2;
   }
-  for (int l = 0; l < kLayers; ++l) {
+  for (int l = 0; l < nl; ++l) {
     f.p[l] = base + off;
     off += rows * kHid;
   }
@@ -532,7 +543,7 @@ static void forward(sg_context *c, const sg_context::PGraph &g, const double2 *v
   pc_scale_kernel<<<nb(len), 256, 0, st>>>(vf, f.u, len, S, f.sq);
   SG_CUDA(cudaGetLastError());
   SG_CUDA(cudaMemcpyAsync(f.h[0], f.u, len * sizeof(float2), cudaMemcpyDeviceToDevice, st));
-  for (int l = 0; l < kLayers; ++l) {
+  for (int l = 0; l < nl; ++l) {
     const LayerOff o = layer_offsets(bs, l);
     pc_apply_kernel<<<n, 256, 0, st>>>(g.G.ptr, g.nbr.ptr, g.k1, bs, S, f.h[l], f.a[l]);
     pc_mlp1_kernel<<<nb(rows, 8), kHid, 8 * 4 * bs * sizeof(float), st>>>(f.a[l], f.h[l], c->p_wb.ptr + o.w1,
@@ -541,7 +552,7 @@ static void forward(sg_context *c, const sg_context::PGraph &g, const double2 *v
                                                    f.u, f.a[l], n, bs, S, f.h[l + 1]);
     SG_CUDA(cudaGetLastError());
   }
-  c->launches += 3 + 3 * kLayers;
+  c->launches += 3 + 3 * nl;
 }
 
 // z = P(v) with the selected graph (double2 vectors, padded [N][B][S])
@@ -551,8 +562,9 @@ void precond_apply(sg_context *c, const double2 *v, double2 *z, int S, cudaStrea
   SG_REQUIRE(g.n == c->n && g.bs == c->bs, "the selected preconditioner graph does not match the particles");
   Fwd f;
   forward(c, g, v, S, f, st);
+  const int nl = c->p_layers;
   const size_t rows = (size_t)g.n * S, len = rows * g.bs;
-  pc_from_f32_scaled<<<nb(len), 256, 0, st>>>(f.h[kLayers], z, len, S, f.sq);
+  pc_from_f32_scaled<<<nb(len), 256, 0, st>>>(f.h[nl], z, len, S, f.sq);
   SG_CUDA(cudaGetLastError());
   c->launches += 1;
 }
@@ -566,6 +578,7 @@ void precond_train(sg_context *c, int gid, const double2 *v, const double2 *e, i
   const size_t rows = (size_t)n * S, len = rows * bs;
   Fwd f;
   forward(c, g, v, S, f, st);
+  const int nl = c->p_layers;
   // dh, da, dhp, tmp (float2 x len each), dg (rows x O), dp (rows x kHid), sq_e (64), loss (1)
   c->p_back.reserve(len * 2 * 4 + rows * O + rows * kHid + 128);
   float *b = c->p_back.ptr;
@@ -574,11 +587,11 @@ void precond_train(sg_context *c, int gid, const double2 *v, const double2 *e, i
   SG_CUDA(cudaMemsetAsync(sq_e, 0, 65 * sizeof(float), st));
   pc_f64_to_f32_kernel<<<nb(len), 256, 0, st>>>(e, tmp, len);
   pc_sqnorm_kernel<<<std::min<unsigned>(nb(len), 1024), 256, S * sizeof(float), st>>>(tmp, len, S, sq_e);
-  pc_loss_kernel<<<nb(len), 256, 0, st>>>(f.h[kLayers], e, f.sq, sq_e, len, S, dh, loss);
+  pc_loss_kernel<<<nb(len), 256, 0, st>>>(f.h[nl], e, f.sq, sq_e, len, S, dh, loss);
   SG_CUDA(cudaGetLastError());
   const int count = c->p_count;
   SG_CUDA(cudaMemsetAsync(c->p_g.ptr, 0, count * sizeof(float), st));
-  for (int l = kLayers - 1; l >= 0; --l) {
+  for (int l = nl - 1; l >= 0; --l) {
     const LayerOff o = layer_offsets(bs, l);
     pc_alpha_back_kernel<<<nb(len), 256, 0, st>>>(f.a[l], dh, c->p_w.ptr + o.al, len, da, c->p_g.ptr + o.al);
     pc_mlp2_back_kernel<<<nb(rows, 8), kHid, 0, st>>>(dh, f.p[l], c->p_wb.ptr + o.w2, n, bs, S, dg, dp);
@@ -590,7 +603,7 @@ void precond_train(sg_context *c, int gid, const double2 *v, const double2 *e, i
     SG_CUDA(cudaGetLastError());
     std::swap(dh, dhp);
   }
-  c->launches += 3 + 7 * kLayers;
+  c->launches += 3 + 7 * nl;
   float hl = 0.f;
   SG_CUDA(cudaMemcpyAsync(&hl, loss, sizeof(float), cudaMemcpyDeviceToHost, st));
   if (grad_host) SG_CUDA(cudaMemcpyAsync(grad_host, c->p_g.ptr, count * sizeof(float), cudaMemcpyDeviceToHost, st));

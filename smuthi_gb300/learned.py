@@ -31,21 +31,36 @@ import scipy.spatial
 from . import _lib
 
 HIDDEN = 128
-LAYERS = 3
+LAYERS = 3        # default depth; the library takes 1..MAX_LAYERS layers (the parameter count sets it)
+MAX_LAYERS = 8
 K_NEIGHBOURS = 16
 DATA_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
 
 
-def param_count(blocksize):
+def per_layer_count(blocksize):
     f, o = 4 * blocksize, 2 * blocksize
-    return LAYERS * (HIDDEN * f + HIDDEN + o * HIDDEN + o + 2)
+    return HIDDEN * f + HIDDEN + o * HIDDEN + o + 2
+
+
+def param_count(blocksize, layers=LAYERS):
+    return layers * per_layer_count(blocksize)
+
+
+def layers_of(params, blocksize):
+    """Depth of a parameter vector (ValueError when its size fits no depth 1..MAX_LAYERS)."""
+    per = per_layer_count(blocksize)
+    n = int(params.shape[0]) if hasattr(params, "shape") else len(params)  # numpy arrays and torch tensors
+    if n % per or not 1 <= n // per <= MAX_LAYERS:
+        raise ValueError("%d parameters fit no network of 1..%d layers for blocksize %d" % (n, MAX_LAYERS,
+                                                                                          blocksize))
+    return n // per
 
 
 def layer_views(params, blocksize):
     """Per layer a dict of views into the flat parameter vector: W1 (128 x 4B), b1, W2 (2B x 128), b2, alpha."""
     f, o = 4 * blocksize, 2 * blocksize
     out, off = [], 0
-    for _ in range(LAYERS):
+    for _ in range(layers_of(params, blocksize)):
         d = {}
         d["W1"] = params[off:off + HIDDEN * f].reshape(HIDDEN, f)
         off += HIDDEN * f
@@ -62,10 +77,10 @@ def layer_views(params, blocksize):
     return out
 
 
-def init_params(blocksize, seed=0):
+def init_params(blocksize, seed=0, layers=LAYERS):
     """Neumann-series start: W2 = b2 = 0, alpha = 1; W1 ~ N(0, 1/(4B))."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    p = np.zeros(param_count(blocksize), np.float32)
+    p = np.zeros(param_count(blocksize, layers), np.float32)
     for d in layer_views(p, blocksize):
         d["W1"][:] = rng.standard_normal(d["W1"].shape) / math.sqrt(d["W1"].shape[1])
         d["alpha"][:] = (1.0, 0.0)
@@ -112,9 +127,7 @@ def load_params(name, blocksize):
     path = os.path.join(DATA_DIR, name + ".npz")
     d = np.load(path)
     p = np.ascontiguousarray(d["params"], dtype=np.float32)
-    if p.size != param_count(blocksize):
-        raise ValueError("%s holds %d parameters, blocksize %d needs %d" % (path, p.size, blocksize,
-                                                                             param_count(blocksize)))
+    layers_of(p, blocksize)  # raises when the size fits no network of this blocksize
     return p
 
 
@@ -245,9 +258,9 @@ def use(system, params, k=K_NEIGHBOURS):
     return gid
 
 
-def alpha_mask(blocksize):
+def alpha_mask(blocksize, layers=LAYERS):
     """Mask selecting only the per-layer alpha coefficients (the near-field polynomial)."""
-    m = np.zeros(param_count(blocksize), np.float32)
+    m = np.zeros(param_count(blocksize, layers), np.float32)
     for d in layer_views(m, blocksize):
         d["alpha"][:] = 1.0
     return m
@@ -287,7 +300,7 @@ def train(system, params, steps=500, lr=1e-3, batch=16, k=K_NEIGHBOURS, pool=Non
         losses.append(loss)
         if log and (it == 1 or it % log_every == 0):
             log("step %d loss %.4f" % (it, float(np.mean(losses[-log_every:]))))
-    out = ctx.precond_get_params(param_count(bs))
+    out = ctx.precond_get_params(p.size)
     ctx.precond_select(gid)
     return out, losses
 
@@ -325,6 +338,166 @@ def evaluate_loss(system, params, pool, batches=8, batch=16, k=K_NEIGHBOURS):
         torch.cuda.synchronize(pool.dev)
         out.append(ctx.precond_train_step(gid, v.data_ptr(), e.data_ptr(), v.shape[1], lr=0.0, step=0))
     return float(np.mean(out))
+
+
+# ------------------------------------------------------------------------------------------- many configurations
+def get_alphas(params, blocksize):
+    """Per-layer alpha coefficients (complex, one per layer)."""
+    return np.array([complex(d["alpha"][0], d["alpha"][1]) for d in layer_views(params, blocksize)])
+
+
+def set_alphas(params, blocksize, alphas):
+    """Copy of ``params`` with the per-layer alpha coefficients replaced."""
+    p = np.array(params, np.float32, copy=True)
+    for d, a in zip(layer_views(p, blocksize), alphas):
+        d["alpha"][:] = (np.float32(np.real(a)), np.float32(np.imag(a)))
+    return p
+
+
+def mean_iterations(systems, params, k=K_NEIGHBOURS, nrhs=16):
+    """Mean FGMRES iteration count of the mixed solve over systems, and whether every solve met the
+    FP64-true tolerance without a preconditioner fallback."""
+    its, ok = [], True
+    for s in systems:
+        info, rel = solve_iterations(s, params, nrhs=nrhs, k=k)
+        its.append(info["iterations"])
+        ok &= info["converged"] == nrhs and float(rel.max()) <= 1e-6 and info["precond_fallbacks"] == 0
+    return float(np.mean(its)), bool(ok)
+
+
+def tune_alphas(systems, params, k=K_NEIGHBOURS, rounds=6, step=0.25, log=print):
+    """Pattern search over the real and imaginary parts of the per-layer alphas (the coefficients of
+    the near-field polynomial the network reduces to with its MLP at zero) minimising the mean FGMRES
+    iteration count over the training systems: the iteration count is what the preconditioner is for,
+    and the regression losses do not track it. Returns (params, history)."""
+    bs = systems[0]["blocksize"]
+    x = np.concatenate([[a.real, a.imag] for a in get_alphas(params, bs)])
+
+    def f(v):
+        p = set_alphas(params, bs, v[0::2] + 1j * v[1::2])
+        it, ok = mean_iterations(systems, p, k)
+        return it if ok else float("inf"), p
+
+    best, bp = f(x)
+    hist = [(x.tolist(), best)]
+    for _ in range(rounds):
+        improved = False
+        for d in range(len(x)):
+            for sgn in (1.0, -1.0):
+                y = x.copy()
+                y[d] += sgn * step
+                fy, py = f(y)
+                hist.append((y.tolist(), fy))
+                if fy < best:
+                    x, best, bp, improved = y, fy, py, True
+                    break
+        log("alpha search: step %.4f, mean iterations %.2f, alphas %s" % (step, best, np.round(x, 3).tolist()))
+        if not improved:
+            step /= 2
+    return bp, hist
+
+
+def krylov_pools(systems, seed=0):
+    """Training pools of mostly-Krylov pairs (exact FP64 pairs of the solved plane waves, a quarter
+    white) for every system."""
+    return [TrainingPool(s, white_fraction=0.25, seed=seed + i) for i, s in enumerate(systems)]
+
+
+def train_multi(systems, pools, params, steps=600, lr=1e-5, batch=16, k=K_NEIGHBOURS, mask=None, log=None,
+                log_every=100):
+    """One network trained on many particle sets: every step takes a batch of one set (in turn), its
+    graph and blocks, and the library's forward and backward kernels on that set's context; the Adam
+    step runs on the host on the shared parameter vector. Returns (params, losses)."""
+    import torch
+    bs = systems[0]["blocksize"]
+    p = np.ascontiguousarray(params, dtype=np.float32).copy()
+    m1, m2 = np.zeros_like(p), np.zeros_like(p)
+    grad = np.zeros_like(p)
+    losses = []
+    for it in range(1, steps + 1):
+        q = (it - 1) % len(systems)
+        s, pool = systems[q], pools[q]
+        gid = graph_for(s, k)
+        s["ctx"].precond_set_params(bs, p)
+        v, e = pool.batch(batch)
+        torch.cuda.synchronize(pool.dev)
+        losses.append(s["ctx"].precond_train_step(gid, v.data_ptr(), e.data_ptr(), v.shape[1], lr=0.0, step=0,
+                                                  grad=grad))
+        g = grad if mask is None else grad * mask
+        m1 = 0.9 * m1 + 0.1 * g
+        m2 = 0.999 * m2 + 0.001 * g * g
+        p = (p - lr * (m1 / (1 - 0.9 ** it)) / (np.sqrt(m2 / (1 - 0.999 ** it)) + 1e-8)).astype(np.float32)
+        if log and (it == 1 or it % log_every == 0):
+            log("multi-set step %d loss %.4f" % (it, float(np.mean(losses[-log_every:]))))
+    return p, losses
+
+
+def film_configurations(name, count, sizes=(500, 750, 1000), seed0=1000):
+    """``count`` seeded configurations of a workload shape with sizes cycling through ``sizes``
+    (same areal density as the shape)."""
+    return [(sizes[i % len(sizes)], seed0 + i) for i in range(count)]
+
+
+def fit_many(name="c5", n_configs=200, n_tune=4, val=(2000, 12), k=K_NEIGHBOURS, log=print):
+    """Train the preconditioner for a workload shape on many seeded configurations and keep the
+    candidate with the fewest FGMRES iterations on a held-out configuration.
+
+    Candidates: the Neumann start; the per-layer alphas tuned for iterations on ``n_tune`` configurations
+    of 1000-2000 spheres (``tune_alphas``); the full network fine-tuned from the tuned alphas on
+    mostly-Krylov pairs of ``n_configs`` configurations of 500-1000 spheres, each solved by the
+    library (``train_multi``), at two learning rates. Returns (params, report)."""
+    import time
+    t0 = time.time()
+    vsys = film_system(name, val[0], nrhs=16, seed=val[1])
+    bs = vsys["blocksize"]
+    base, _ = solve_iterations(vsys)
+    report = {"shape": name, "n_configs": n_configs, "n_tune": n_tune, "val": list(val), "k": k,
+              "val_unpreconditioned": base}
+    log("held-out, unpreconditioned: %d iterations" % base["iterations"])
+    cands = {"neumann": init_params(bs)}
+    tune = [film_system(name, n, nrhs=16, seed=s) for n, s in film_configurations(name, n_tune, (1000, 2000), 500)]
+    cands["alphas_tuned"], hist = tune_alphas(tune, cands["neumann"], k=k, log=log)
+    report["alpha_search"] = {"evaluations": len(hist), "best_mean_iterations": min(h[1] for h in hist),
+                              "start_mean_iterations": hist[0][1],
+                              "alphas": [[float(a.real), float(a.imag)] for a in get_alphas(cands["alphas_tuned"], bs)]}
+    for s in tune:
+        s["ctx"].close()
+    systems, pools = [], []
+    for n, s in film_configurations(name, n_configs):
+        sysm = film_system(name, n, nrhs=16, seed=s)
+        systems.append(sysm)
+        pools.append(TrainingPool(sysm, white_fraction=0.25, seed=s))
+    report["train_data_s"] = round(time.time() - t0, 1)
+    for lr in (1e-5, 3e-5):
+        cands["full_multi_%g" % lr], losses = train_multi(systems, pools, cands["alphas_tuned"], steps=2 * n_configs,
+                                                          lr=lr, k=k, log=log)
+        report["loss_full_multi_%g" % lr] = [float(np.mean(losses[:20])), float(np.mean(losses[-20:]))]
+    for s in systems:
+        s["ctx"].close()
+    del pools
+    best, best_it = None, None
+    for tag, p in cands.items():
+        info, rel = solve_iterations(vsys, p, k=k)
+        report["val_" + tag] = info
+        ok = info["converged"] == 16 and float(rel.max()) <= 1e-6 and info["precond_fallbacks"] == 0
+        log("%s: %d held-out iterations, %.3f s, ok %s" % (tag, info["iterations"], info["device_seconds"], ok))
+        if ok and (best_it is None or info["iterations"] < best_it):
+            best, best_it = tag, info["iterations"]
+    report["selected"] = best or "neumann"
+    best = report["selected"]
+    best_k, best_kit = k, best_it
+    for kk in (24, 32, 48):
+        info, rel = solve_iterations(vsys, cands[best], k=kk)
+        report["val_k%d" % kk] = info
+        ok = info["converged"] == 16 and float(rel.max()) <= 1e-6 and info["precond_fallbacks"] == 0
+        log("%s at k=%d: %d iterations, %.3f s, ok %s" % (best, kk, info["iterations"], info["device_seconds"], ok))
+        if ok and best_kit is not None and info["iterations"] < best_kit:
+            best_k, best_kit = kk, info["iterations"]
+    report["k"] = best_k
+    report["neumann_same_k"] = solve_iterations(vsys, cands["neumann"], k=best_k)[0]
+    report["wall_s"] = round(time.time() - t0, 1)
+    vsys["ctx"].close()
+    return cands[best], report
 
 
 # ------------------------------------------------------------------------------------------- weights
@@ -386,8 +559,14 @@ def main(argv=None):
     ap.add_argument("--n-val", type=int, default=2000)
     ap.add_argument("--out", default=None, help="weights name (default precond_<shape>)")
     ap.add_argument("--dir", default=None, help="output directory (default: the package data directory)")
+    ap.add_argument("--many", type=int, default=0,
+                    help="train on this many seeded configurations (fit_many) instead of one ensemble")
+    ap.add_argument("--tune", type=int, default=4, help="configurations of the alpha search (with --many)")
     a = ap.parse_args(argv)
-    p, rep = fit_film_weights(a.shape, a.n_train, a.n_val)
+    if a.many:
+        p, rep = fit_many(a.shape, a.many, a.tune, (a.n_val, 12))
+    else:
+        p, rep = fit_film_weights(a.shape, a.n_train, a.n_val)
     name = a.out or "precond_%s" % a.shape
     path = save_params(p, name, meta={"report": json.dumps(rep, default=float), "k": np.int32(rep["k"])},
                        directory=a.dir)

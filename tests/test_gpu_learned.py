@@ -221,14 +221,18 @@ def test_precond_argument_checks(gpu_context):
 
 
 def test_committed_weights_reduce_iterations_on_held_out_film(gpu_context):
-    """The shipped weights (selected on another particle set) cut the mixed solve's iterations on a
-    film ensemble none of the training or selection runs saw, at the same FP64-true tolerance."""
+    """The shipped film weights (trained on 200 seeded configurations, selected and tuned on others)
+    need fewer mixed-solve iterations than their untrained start, the near-field Neumann series on the
+    same graph, which needs fewer than no preconditioner: trained < Neumann < none on a film ensemble
+    none of the training, tuning or selection runs saw, at the same FP64-true tolerance."""
     from smuthi_gb300 import learned
     val = learned.film_system("c5", 1000, nrhs=16, seed=31, ctx=gpu_context)
-    weights = learned.load_params("precond_c5", val["blocksize"])
+    bs = val["blocksize"]
+    weights = learned.load_params("precond_c5", bs)
     k = learned.load_meta("precond_c5")["k"]
     base, rel0 = learned.solve_iterations(val)
+    neumann, reln = learned.solve_iterations(val, learned.init_params(bs), k=k)
     info, rel = learned.solve_iterations(val, weights, k=k)
-    assert rel0.max() <= 1e-6 and rel.max() <= 1e-6
+    assert rel0.max() <= 1e-6 and reln.max() <= 1e-6 and rel.max() <= 1e-6
     assert info["converged"] == 16 and info["precond_fallbacks"] == 0
-    assert info["iterations"] < base["iterations"]
+    assert info["iterations"] < neumann["iterations"] < base["iterations"]
