@@ -1,9 +1,8 @@
 """Generate golden fixtures by running the reference SMUTHI code itself.
 
-Run in a container that holds the reference source tree (default
-``/root/reference``, override with ``SMUTHI_REFERENCE_ROOT``)::
+Run where the reference source tree is available, naming it in ``SMUTHI_REFERENCE_ROOT``::
 
-    python tests/golden/make_golden.py [case ...]
+    SMUTHI_REFERENCE_ROOT=/root/reference python tests/golden/make_golden.py [case ...]
 
 The reference is imported with the three test-only shims of ``refload.py``.
 Each case writes ``tests/golden/<case>.npz`` with the inputs (geometry,

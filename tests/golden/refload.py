@@ -19,7 +19,7 @@ import sys
 import numpy as np
 import scipy.sparse.linalg
 
-REFERENCE_ROOT = os.environ.get("SMUTHI_REFERENCE_ROOT", "/root/reference")
+REFERENCE_ROOT = os.environ.get("SMUTHI_REFERENCE_ROOT")  # the reference checkout that generates fixtures
 _HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -41,6 +41,9 @@ def _install_shims():
 
 def import_reference():
     """Return the reference ``smuthi`` package (imported with the shims)."""
+    if not REFERENCE_ROOT:
+        raise RuntimeError("set SMUTHI_REFERENCE_ROOT to the reference source checkout (the directory holding "
+                           "the smuthi package) to generate fixtures")
     if not os.path.isdir(os.path.join(REFERENCE_ROOT, "smuthi")):
         raise RuntimeError("reference source tree not found at " + REFERENCE_ROOT)
     shim = os.path.join(_HERE, "refshim")
