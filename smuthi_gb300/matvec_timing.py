@@ -12,6 +12,12 @@ times the volume-lookup operator instead: spheres (radius 60 nm) on a jittered 2
 lattice at seeded heights in [100, 160] nm above a glass substrate, 550 nm, 10 nm lookup grid. It is also the small, fixed launch sequence used to profile
 one coupling kernel: the first operator application carries one-time set-up (pair table, double-float
 coefficients, FP32 kernel autotuning), the later ones are steady state.
+
+    python -m smuthi_gb300.matvec_timing --nearfield 16384 --repeat 3
+
+times the electric field of a seeded upgoing plane-wave expansion (550 nm in air above glass, the
+default Sommerfeld contour and azimuth grid) at that many points above the particles' plane, host
+copies included (`sg_pwe_field`).
 """
 import argparse
 import json
@@ -49,6 +55,33 @@ def volume_system(n, nrhs, kind, seed=0):
                 table_shape=list(W.lookup_table_plus.shape))
 
 
+def nearfield_timing(n_points, repeat, seed=0):
+    """Seconds per electric-field evaluation of a seeded plane-wave expansion at n_points (see above)."""
+    import time
+    from . import fields as flds
+    from . import layers
+    from .fields.expansions import PlaneWaveExpansion
+    rng = np.random.default_rng(seed)
+    ls = layers.LayerSystem([0, 0], [1.52, 1])
+    wl = 550.0
+    kp = flds.reasonable_Sommerfeld_kpar_contour(wl, layer_refractive_indices=ls.refractive_indices)
+    az, _ = flds.angular_arrays(np.pi / 360)
+    k = flds.angular_frequency(wl)
+    pwe = PlaneWaveExpansion(k, kp, az, kind='upgoing', reference_point=[0, 0, 100.0], lower_z=100.0)
+    pwe.coefficients = rng.standard_normal((2, len(kp), len(az))) + 1j * rng.standard_normal((2, len(kp), len(az)))
+    x, y = rng.uniform(-2000, 2000, n_points), rng.uniform(-2000, 2000, n_points)
+    z = rng.uniform(300, 1000, n_points)
+    ctx = _lib.Context(0)
+    pwe.electric_field(x, y, z, context=ctx)  # warm-up
+    t = time.perf_counter()
+    for _ in range(repeat):
+        pwe.electric_field(x, y, z, context=ctx)
+    dt = (time.perf_counter() - t) / repeat
+    ctx.close()
+    return {"nearfield_points": n_points, "k_parallel_nodes": len(kp), "azimuths": len(az), "seconds": dt,
+            "ns_per_point_and_node": dt / (n_points * len(kp) * len(az)) * 1e9}
+
+
 def main(argv=None):
     import torch
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
@@ -59,10 +92,15 @@ def main(argv=None):
     ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--volume", action="store_true", help="time the volume lookup (particles at different heights)")
     ap.add_argument("--kind", default="linear", choices=("linear", "cubic", "cubic_hermite"))
+    ap.add_argument("--nearfield", type=int, default=0, metavar="POINTS",
+                    help="time the near field of a plane-wave expansion at this many points instead")
     ap.add_argument("--fp32-kernel", default=None, metavar="VARIANT:TILE",
                     help="fix the FP32 kernel (0 per-receiver, 1 bucketed, 2 pair-symmetric) and its RHS tile "
                          "instead of the autotuner's choice")
     a = ap.parse_args(argv)
+    if a.nearfield:
+        print(json.dumps(nearfield_timing(a.nearfield, a.repeat)))
+        return
     if a.volume:
         system = volume_system(a.n_spheres or 1000, a.nrhs, a.kind)
     else:
