@@ -30,6 +30,8 @@
 
 #include "sg_internal.h"
 
+#include <type_traits>
+
 namespace sg {
 
 template <typename Real>
@@ -73,6 +75,38 @@ __device__ __forceinline__ int axis_taps(double coord, double origin, double res
     const double s = 1.0 - t;
     wm[0] = (s * s * s - s) / 6.0;
     wm[1] = (t * t * t - t) / 6.0;
+  }
+  return i;
+}
+
+// The same taps for the FP32 operator: only the grid coordinate u = (coord - origin) / res and its
+// integer part are formed in FP64 (they set which cells are read); the weights, polynomials of the
+// fraction t in [0, 1), are evaluated in FP32, so the FP64 pipe (1/59 of the FP32 rate on GB300)
+// carries a few operations per pair instead of the whole tap set.
+template <int KIND>
+__device__ __forceinline__ int axis_taps_f32(double coord, double origin, double inv_res, int len, float *wv,
+                                             float *wm) {
+  const double u = (coord - origin) * inv_res;
+  int i = (int)floor(u);
+  if (KIND == SG_CUBIC_HERMITE) {
+    i = i < 1 ? 1 : (i > len - 3 ? len - 3 : i);
+    const float w = (float)(u - i);
+    wv[0] = 0.5f * (-w * w * w + 2.f * w * w - w);
+    wv[1] = 0.5f * (3.f * w * w * w - 5.f * w * w + 2.f);
+    wv[2] = 0.5f * (-3.f * w * w * w + 4.f * w * w + w);
+    wv[3] = 0.5f * (w * w * w - w * w);
+    return i - 1;
+  }
+  i = i < 0 ? 0 : (i > len - 2 ? len - 2 : i);
+  const float t = (float)(u - i);
+  wv[0] = 1.f - t;
+  wv[1] = t;
+  if (KIND == SG_CUBIC) {
+    const float s = 1.f - t;
+    wm[0] = (s * s * s - s) * (1.f / 6.f);
+    wm[1] = (t * t * t - t) * (1.f / 6.f);
+  } else {
+    wm[0] = wm[1] = 0.f;
   }
   return i;
 }
@@ -188,6 +222,121 @@ __global__ void __launch_bounds__(kVolThreads) volume_kernel(const VolumeLaunch 
   }
   const int per = (N + nsplit - 1) / nsplit;
   const int j0 = split * per, j1 = min(N, j0 + per);
+  constexpr bool F32 = std::is_same<Real, float>::value;
+  // FP32 operator: the rotated pair sums accumulate in registers across the warp's pairs
+  float2 tot[NB1][RT];
+#pragma unroll
+  for (int s = 0; s < NB1; ++s)
+#pragma unroll
+    for (int r = 0; r < RT; ++r) tot[s][r] = make_float2(0.f, 0.f);
+  const double inv_res = 1.0 / V.res;
+  if constexpr (F32) {
+  for (int j = j0 + warp; j < j1; j += nw) {
+    const double2 pj = L.pos[j];
+    const double dx = pi.x - pj.x, dy = pi.y - pj.y;
+    const double rho = sqrt(dx * dx + dy * dy);
+    const double zj = V.z[j];
+    float wr[NT], wrm[2], wp[NT], wpm[2], wn[NT], wnm[2];
+    const int ir = axis_taps_f32<KIND>(rho, V.rho_min, inv_res, V.len_rho, wr, wrm);
+    const int ip = axis_taps_f32<KIND>(zi + zj, V.sz_min, inv_res, V.len_z, wp, wpm);
+    const int im = axis_taps_f32<KIND>(zi - zj, V.dz_min, inv_res, V.len_z, wn, wnm);
+    float c = 1.f, sn = 0.f;
+    if (rho > 0.0) {
+      const double ir_ = 1.0 / rho;
+      c = (float)(dx * ir_);
+      sn = (float)(dy * ir_);
+    }
+    // e^{i m phi} of the lane's rows by repeated multiplication; x_j (FP32 copy) staged with e^{i m2 phi}
+    float pr[NB1], pim[NB1];
+#pragma unroll
+    for (int s = 0; s < NB1; ++s) {
+      const int am = m1[s] < 0 ? -m1[s] : m1[s];
+      float a = 1.f, b = 0.f;
+      for (int q = 0; q < am; ++q) {
+        const float na = a * c - b * sn;
+        b = a * sn + b * c;
+        a = na;
+      }
+      pr[s] = a;
+      pim[s] = m1[s] < 0 ? -b : b;
+    }
+#pragma unroll
+    for (int s = 0; s < NB1; ++s) {
+      const int n2 = lane + 32 * s;
+      if (n2 < bs) {
+        const float2 *xr = L.x32 + ((size_t)j * bs + n2) * R + r0;
+#pragma unroll
+        for (int r = 0; r < RT; ++r) {
+          cplx v;
+          if (r < nr) {
+            const float2 xv = __ldg(xr + r);
+            v.x = pr[s] * xv.x - pim[s] * xv.y;
+            v.y = pr[s] * xv.y + pim[s] * xv.x;
+          } else {
+            v.x = 0;
+            v.y = 0;
+          }
+          xs[n2 * RT + r] = v;
+        }
+      }
+    }
+    __syncwarp();
+    const cplx *rp[NT], *rm[NT];
+#pragma unroll
+    for (int a = 0; a < NT; ++a) {
+      rp[a] = Tp + (size_t)(ir + a) * rs + (size_t)ip * zs;
+      rm[a] = Tm + (size_t)(ir + a) * rs + (size_t)im * zs;
+    }
+    cplx acc[NB1][RT];
+#pragma unroll
+    for (int s = 0; s < NB1; ++s)
+#pragma unroll
+      for (int r = 0; r < RT; ++r) {
+        acc[s][r].x = 0;
+        acc[s][r].y = 0;
+      }
+    for (int n2 = 0; n2 < bs; ++n2) {
+#pragma unroll
+      for (int s = 0; s < NB1; ++s) {
+        const int n1 = lane + 32 * s;
+        if (n1 < bs) {
+          const cplx *pa[NT], *ma[NT];
+#pragma unroll
+          for (int a = 0; a < NT; ++a) {
+            pa[a] = rp[a] + n2 * bs + n1;
+            ma[a] = rm[a] + n2 * bs + n1;
+          }
+          const cplx wpl = table_value<Real, KIND, NT>(pa, zs, qs, wr, wrm, wp, wpm);
+          const cplx wmn = table_value<Real, KIND, NT>(ma, zs, qs, wr, wrm, wn, wnm);
+          const Real wre = wpl.x + wmn.x, wim = wpl.y + wmn.y;
+#pragma unroll
+          for (int r = 0; r < RT; ++r) {
+            const cplx xv = xs[n2 * RT + r];
+            acc[s][r].x += wre * xv.x - wim * xv.y;
+            acc[s][r].y += wre * xv.y + wim * xv.x;
+          }
+        }
+      }
+    }
+    // rotate by e^{-i m1 phi} into the register accumulator
+#pragma unroll
+    for (int s = 0; s < NB1; ++s)
+#pragma unroll
+      for (int r = 0; r < RT; ++r) {
+        const float ar = (float)acc[s][r].x, ai = (float)acc[s][r].y;
+        tot[s][r].x += pr[s] * ar + pim[s] * ai;
+        tot[s][r].y += pr[s] * ai - pim[s] * ar;
+      }
+    __syncwarp();  // xs is rewritten by the next pair
+  }
+#pragma unroll
+  for (int s = 0; s < NB1; ++s) {
+    const int n1 = lane + 32 * s;
+    if (n1 < bs)
+#pragma unroll
+      for (int r = 0; r < RT; ++r) myacc[n1 * RT + r] = make_double2((double)tot[s][r].x, (double)tot[s][r].y);
+  }
+  } else {
   for (int j = j0 + warp; j < j1; j += nw) {
     const double2 pj = L.pos[j];
     const double dx = pi.x - pj.x, dy = pi.y - pj.y;
@@ -290,6 +439,7 @@ __global__ void __launch_bounds__(kVolThreads) volume_kernel(const VolumeLaunch 
       }
     }
     __syncwarp();  // xs is rewritten by the next pair
+  }
   }
   __syncthreads();
   double2 *red = reinterpret_cast<double2 *>(vsmem);  // reuses the staging area
@@ -504,6 +654,14 @@ int launch_volume(sg_context *c, const double2 *x, double2 *y, int R, bool maste
   L.t = c->tmat.ptr;
   L.ptype = c->ptype.ptr;
   L.t_diag = c->t_diag;
+  int extra = 0;
+  if (fp32) {  // one FP32 copy of the input: the kernel stages x_j from it
+    const size_t len = (size_t)c->n * c->bs * R;
+    c->bk_x32.reserve(len);
+    k_to_f32(x, c->bk_x32.ptr, len, st);
+    L.x32 = c->bk_x32.ptr;
+    extra = 1;
+  }
   V.z = c->vz.ptr;
   V.tpl = fp32 ? (const void *)c->vpl32.ptr : (const void *)c->vpl64.ptr;
   V.tmn = fp32 ? (const void *)c->vmn32.ptr : (const void *)c->vmn64.ptr;
@@ -521,7 +679,7 @@ int launch_volume(sg_context *c, const double2 *x, double2 *y, int R, bool maste
   }
   if (fp32) launch_vr<float>(V, c->kind, ns, st);
   else launch_vr<double>(V, c->kind, ns, st);
-  return ns > 1 ? 2 : 1;
+  return (ns > 1 ? 2 : 1) + extra;
 }
 
 }  // namespace sg
