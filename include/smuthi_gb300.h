@@ -52,10 +52,12 @@ extern "C" {
  * FP64 operator. No counterpart in the reference. */
 #define SG_DF64 8
 /* matvec precision: the coupling operator on the tensor cores (tcgen05.mma kind::tf32, each
- * operand split into a TF32 high part and a remainder, three products), for blocksize <= 32,
- * uniform particles, diagonal T and nrhs in {8, 16, 32}. Relative error 2e-6 to 1e-5 on systems of
- * up to ~120 particles, growing with the particle count (the accumulation in tensor memory is not
- * round-to-nearest FP32), so it is not used by the solver. No counterpart in the reference. */
+ * operand split into a TF32 high part and a remainder, three products), for the radial lookup with
+ * blocksize <= 48 and nrhs in {16, 32, 64}. Each tensor-memory accumulator takes a few emitters
+ * before it is added into an FP32 total (round-to-nearest), which bounds the error of the tensor
+ * core's accumulation. It is also variant 4 of the FP32 operator (sg_fp32_autotune /
+ * sg_fp32_set_kernel), the inner operator of the mixed-precision solve when it is the fastest.
+ * No counterpart in the reference. */
 #define SG_TF32X3 16
 
 typedef struct sg_context sg_context;
@@ -170,22 +172,29 @@ int sg_launch_count(sg_context *ctx, int64_t *count);
 /* FP32-operator autotuner result for an RHS count: variant 0 = per-receiver kernel, 1 =
  * interval-bucketed kernel, 2 = pair-symmetric kernel (one interpolation per unordered pair serves
  * both directions; one warp per receiver), 3 = the pair-symmetric kernel with two warps per receiver
- * (each half of the RHS tile), -1 = not tuned yet; rhs_tile = the chosen kernel's RHS tile per CTA; with the
- * CUDA-event times (ms) of one run of the best per-receiver tile, of the bucketed kernel and of the
- * best pair-symmetric tile (-1 when not a candidate). The first FP32 application for a new RHS count
- * times every candidate on the live operands (synchronising the stream) and keeps the fastest. No
- * counterpart in the reference. */
+ * (each half of the RHS tile), 4 = the tensor-core operator (SG_TF32X3), -1 = not tuned yet;
+ * rhs_tile = the chosen kernel's RHS tile per CTA (nrhs for variant 4); with the CUDA-event times
+ * (ms) of one run of the best per-receiver tile, of the bucketed kernel, of the best pair-symmetric
+ * tile and of the tensor-core operator (-1 when not a candidate; any output pointer may be NULL).
+ * The first FP32 application for a new RHS count times every candidate on the live operands
+ * (synchronising the stream) and keeps the fastest. No counterpart in the reference. */
 int sg_fp32_autotune(sg_context *ctx, int nrhs, int *variant, int *rhs_tile, double *ms_receiver,
-                     double *ms_bucket, double *ms_symmetric);
+                     double *ms_bucket, double *ms_symmetric, double *ms_tensor);
 
 /* Fixes the FP32 operator for an RHS count instead of timing the candidates: variant 0 =
  * per-receiver kernel (rhs_tile 1, 2, 4, 8 or 16 dividing nrhs), 1 = interval-bucketed kernel
  * (rhs_tile ignored; needs its plan), 2 = pair-symmetric kernel (rhs_tile a power of two dividing
  * nrhs, at most 16 for blocksize <= 32 and 8 for blocksize <= 64), 3 = pair-symmetric kernel with two
- * warps per receiver (the same tiles, at least 4). Replaces an earlier choice for
+ * warps per receiver (the same tiles, at least 4), 4 = tensor-core operator (rhs_tile = nrhs, in
+ * {16, 32, 64}; blocksize <= 48). Replaces an earlier choice for
  * that RHS count; set_particles / set_lookup clear it. For tests and measurements of one kernel; no
  * counterpart in the reference. */
 int sg_fp32_set_kernel(sg_context *ctx, int nrhs, int variant, int rhs_tile);
+
+/* Emitters accumulated into one tensor-memory accumulator of the tensor-core operator before it is
+ * added into the FP32 total (default 8). Fewer emitters bound the tensor core's accumulation error
+ * more tightly at the cost of more drains. No counterpart in the reference. */
+int sg_tc_set_window(sg_context *ctx, int emitters);
 
 /* FMA throughput (TFLOP/s, 2 flops per FMA) of the FP64 or FP32 pipe of the
  * context's device, measured with a dependent-chain probe kernel. Used to

@@ -28,7 +28,7 @@ EXPORTS = ("sg_last_error", "sg_version", "sg_create", "sg_destroy", "sg_set_par
            "sg_set_tmatrix", "sg_coupling_matvec", "sg_master_matvec", "sg_coupling_matvec_dev",
            "sg_master_matvec_dev", "sg_gmres_solve", "sg_gmres_solve_dev", "sg_true_residual", "sg_profile",
            "sg_kernel_timing", "sg_launch_count", "sg_measure_fma_peak", "sg_fp32_autotune", "sg_fp32_set_kernel",
-           "sg_coupling_matvec_linear_noalloc", "sg_precond_param_count", "sg_precond_add_graph",
+           "sg_tc_set_window", "sg_coupling_matvec_linear_noalloc", "sg_precond_param_count", "sg_precond_add_graph",
            "sg_precond_select", "sg_precond_clear", "sg_precond_set_params", "sg_precond_get_params",
            "sg_precond_apply_dev", "sg_precond_train_step", "sg_precond_export_blocks", "sg_bessel_jac_table",
            "sg_lookup_contract",
@@ -88,8 +88,9 @@ def _declare(L):
         "sg_launch_count": [_P, ctypes.POINTER(ctypes.c_int64)],
         "sg_measure_fma_peak": [_P, _I, ctypes.POINTER(_D)],
         "sg_fp32_autotune": [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D),
-                             ctypes.POINTER(_D)],
+                             ctypes.POINTER(_D), ctypes.POINTER(_D)],
         "sg_fp32_set_kernel": [_P, _I, _I, _I],
+        "sg_tc_set_window": [_P, _I],
         "sg_coupling_matvec_linear_noalloc": [_I, _I, _P, _I, _P, _I, _D, _D, _P, _P, _P, _I, _P],
         "sg_bessel_jac_table": [_P, _P, _P, _I, _P, _I, _I, _P, _P],
         "sg_lookup_contract": [_P, _P, _I, _I, _P, _I, _P, _D, _D, _P, ctypes.c_longlong, _P],
@@ -257,22 +258,25 @@ class Context:
         return out.value
 
     def fp32_autotune(self, nrhs):
-        """(variant, RHS tile, ms best per-receiver tile, ms bucketed, ms best pair-symmetric tile) for an
-        RHS count; variant -1 if not tuned yet (0 per-receiver, 1 bucketed, 2 pair-symmetric, 3 pair-symmetric
-        with two warps per receiver), a time is -1 when that kernel is not a candidate."""
+        """(variant, RHS tile, ms best per-receiver tile, ms bucketed, ms best pair-symmetric tile, ms tensor
+        cores) for an RHS count; variant -1 if not tuned yet (0 per-receiver, 1 bucketed, 2 pair-symmetric,
+        3 pair-symmetric with two warps per receiver, 4 tensor cores), a time is -1 when that kernel is not a
+        candidate."""
         v = ctypes.c_int()
         t = ctypes.c_int()
-        a = ctypes.c_double()
-        b = ctypes.c_double()
-        c = ctypes.c_double()
-        check(lib().sg_fp32_autotune(self.h, int(nrhs), ctypes.byref(v), ctypes.byref(t), ctypes.byref(a),
-                                     ctypes.byref(b), ctypes.byref(c)))
-        return v.value, t.value, a.value, b.value, c.value
+        ms = [ctypes.c_double() for _ in range(4)]
+        check(lib().sg_fp32_autotune(self.h, int(nrhs), ctypes.byref(v), ctypes.byref(t),
+                                     *[ctypes.byref(m) for m in ms]))
+        return (v.value, t.value) + tuple(m.value for m in ms)
 
     def fp32_set_kernel(self, nrhs, variant, rhs_tile=0):
         """Fix the FP32 operator for an RHS count (0 per-receiver, 1 bucketed, 2 pair-symmetric, 3 pair-symmetric
-        with two warps per receiver)."""
+        with two warps per receiver, 4 tensor cores with rhs_tile = nrhs)."""
         check(lib().sg_fp32_set_kernel(self.h, int(nrhs), int(variant), int(rhs_tile)))
+
+    def tc_set_window(self, emitters):
+        """Emitters per tensor-memory accumulator of the tensor-core operator before it is drained."""
+        check(lib().sg_tc_set_window(self.h, int(emitters)))
 
     # -- learned preconditioner
     def precond_add_graph(self, nbr):

@@ -364,7 +364,7 @@ static void matvec_dev(sg_context *c, const double2 *x, double2 *y, int R, int p
     sg::apply_padded_df64(c, xp, yp, R, master, st);
   } else if (precision == SG_TF32X3) {
     SG_REQUIRE(sg::tc_supported(c, R),
-               "SG_TF32X3 needs blocksize <= 32, uniform particles, diagonal T and nrhs in {8, 16, 32}");
+               "SG_TF32X3 needs the radial lookup, blocksize <= 48 and nrhs in {16, 32, 64}");
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (c->profiling) {
       SG_CUDA(cudaEventCreate(&e0));
@@ -403,6 +403,8 @@ static int matvec_host(sg_context *ctx, const double *x, double *y, int nrhs, in
     SG_CUDA(cudaStreamSynchronize(st));
     if (precision == SG_FP32 && sg::sym_check_error(ctx, st))
       throw sg::Error{SG_ERR_CUDA, "pair-symmetric FP32 operator: a bounded wait ran out"};
+    if (precision == SG_FP32 && sg::tc_check_error(ctx, st))
+      throw sg::Error{SG_ERR_CUDA, "tensor-core operator: a bounded wait ran out"};
     return SG_OK;
   });
 }
@@ -475,6 +477,8 @@ static int solve_dev_impl(sg_context *ctx, const double2 *b, double2 *x, int nrh
   if (info) *info = local;
   if ((precision & SG_FP32) && sg::sym_check_error(ctx, st))
     throw sg::Error{SG_ERR_CUDA, "pair-symmetric FP32 operator: a bounded wait ran out"};
+  if ((precision & SG_FP32) && sg::tc_check_error(ctx, st))
+    throw sg::Error{SG_ERR_CUDA, "tensor-core operator: a bounded wait ran out"};
   if (!std::isfinite(local.max_rel_residual)) throw sg::Error{SG_ERR_NAN, "solver produced NaN or Inf"};
   if (local.converged < nrhs) {
     sg::set_error("GMRES did not reach the tolerance for every right-hand side");
@@ -590,19 +594,29 @@ int sg_measure_fma_peak(sg_context *ctx, int precision, double *tflops) {
 }
 
 int sg_fp32_autotune(sg_context *ctx, int nrhs, int *variant, int *rhs_tile, double *ms_receiver,
-                     double *ms_bucket, double *ms_symmetric) {
+                     double *ms_bucket, double *ms_symmetric, double *ms_tensor) {
   return guarded([&]() -> int {
     SG_REQUIRE(ctx && variant, "null argument");
     for (const auto &t : ctx->tuned)
       if (t.nrhs == nrhs) {
         *variant = t.variant;
-        if (rhs_tile) *rhs_tile = t.variant >= 2 ? t.sym_rt : t.rt;
+        if (rhs_tile) *rhs_tile = t.variant == 4 ? nrhs : (t.variant >= 2 ? t.sym_rt : t.rt);
         if (ms_receiver) *ms_receiver = t.ms_receiver;
         if (ms_bucket) *ms_bucket = t.ms_bucket;
         if (ms_symmetric) *ms_symmetric = t.ms_sym;
+        if (ms_tensor) *ms_tensor = t.ms_tc;
         return SG_OK;
       }
     *variant = -1;
+    return SG_OK;
+  });
+}
+
+int sg_tc_set_window(sg_context *ctx, int emitters) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx, "null context");
+    SG_REQUIRE(emitters >= 1, "the drain window must be at least one emitter");
+    ctx->tc_win = emitters;
     return SG_OK;
   });
 }
@@ -612,10 +626,10 @@ int sg_fp32_set_kernel(sg_context *ctx, int nrhs, int variant, int rhs_tile) {
     SG_REQUIRE(ctx, "null context");
     SG_REQUIRE(nrhs >= 1, "nrhs must be >= 1");
     SG_REQUIRE(!ctx->vol && ctx->kind >= 0, "a radial lookup must be set");
-    SG_REQUIRE(variant >= 0 && variant <= 3, "variant must be 0, 1, 2 or 3");
+    SG_REQUIRE(variant >= 0 && variant <= 4, "variant must be 0, 1, 2, 3 or 4");
     use_device(ctx);
     ensure_pairs(ctx, ctx->stream);  // builds the FP32 operator data now (it would clear the choice later)
-    sg_context::Tuned t{nrhs, variant, 0, -1.f, -1.f, 0, -1.f};
+    sg_context::Tuned t{nrhs, variant, 0, -1.f, -1.f, 0, -1.f, -1.f};
     if (variant == 0) {
       SG_REQUIRE(rhs_tile == 1 || rhs_tile == 2 || rhs_tile == 4 || rhs_tile == 8 || rhs_tile == 16,
                  "per-receiver RHS tile must be 1, 2, 4, 8 or 16");
@@ -623,6 +637,9 @@ int sg_fp32_set_kernel(sg_context *ctx, int nrhs, int variant, int rhs_tile) {
       t.rt = rhs_tile;
     } else if (variant == 1) {
       SG_REQUIRE(ctx->use_bucket, "the bucketed kernel has no plan for this geometry");
+    } else if (variant == 4) {
+      SG_REQUIRE(sg::tc_supported(ctx, nrhs), "the tensor-core operator needs blocksize <= 48 and nrhs in {16, 32, 64}");
+      SG_REQUIRE(rhs_tile == nrhs, "the tensor-core operator takes all right-hand sides at once (rhs_tile = nrhs)");
     } else {
       SG_REQUIRE(sg::sym_supported(ctx), "the pair-symmetric kernel needs blocksize <= 64");
       SG_REQUIRE(rhs_tile >= 1 && rhs_tile <= sg::sym_max_tile(ctx) && (rhs_tile & (rhs_tile - 1)) == 0,

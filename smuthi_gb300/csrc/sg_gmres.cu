@@ -1125,6 +1125,9 @@ static int autotune_fp32(sg_context *c, const double2 *x, double2 *y, int R, boo
       }
     }
   }
+  // the tensor-core operator (3xTF32, accumulators drained every few emitters)
+  float ms_tc = -1.f;
+  if (tc_supported(c, R)) ms_tc = time_it([&] { c->launches += launch_tc_matvec(c, x, y, R, master, st); });
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   int v = 0;
@@ -1133,8 +1136,12 @@ static int autotune_fp32(sg_context *c, const double2 *x, double2 *y, int R, boo
     v = 1;
     best = ms_bucket;
   }
-  if (ms_sym >= 0.f && ms_sym < best) v = sym_split == 2 ? 3 : 2;
-  c->tuned.push_back({R, v, best_rt, best_rec, ms_bucket, sym_rt, ms_sym});
+  if (ms_sym >= 0.f && ms_sym < best) {
+    v = sym_split == 2 ? 3 : 2;
+    best = ms_sym;
+  }
+  if (ms_tc >= 0.f && ms_tc < best) v = 4;
+  c->tuned.push_back({R, v, best_rt, best_rec, ms_bucket, sym_rt, ms_sym, ms_tc});
   return v;
 }
 
@@ -1163,7 +1170,9 @@ void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool maste
       sym_rt = c->tuned.back().sym_rt;
     }
   }
-  if (variant == 2 || variant == 3) {
+  if (variant == 4) {
+    c->launches += launch_tc_matvec(c, x, y, R, master, st);
+  } else if (variant == 2 || variant == 3) {
     c->launches += launch_sym_matvec(c, x, y, R, master, sym_rt, variant == 3 ? 2 : 1, st);
   } else if (variant == 1) {
     c->launches += launch_bucket_matvec(c, x, y, R, master, st);

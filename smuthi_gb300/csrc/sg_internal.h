@@ -93,6 +93,8 @@ void k_to_df64(const double2 *x, void *xdf, size_t n, cudaStream_t st);
 bool tc_supported(const sg_context *c, int R);
 int launch_tc_matvec(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st);
 bool tc_check_error(sg_context *c, cudaStream_t st);  // reads and clears the timeout flag (synchronises)
+// FP32 W x in c->sym_yacc -> FP64 W x or x - T (W x) (diagonal or dense T); one launch
+void launch_fp32_epilogue(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st);
 // y = M x or W x in double-float arithmetic (FP64-grade; builds the df64 coefficients on first use)
 void apply_padded_df64(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st);
 // padded-vector operator application and solver (sg_gmres.cu)
@@ -217,6 +219,7 @@ struct sg_context {
   sg::DevBuf<float> tc_xop;  // tensor-core operator: pre-split TF32 hi/lo RHS panels
   sg::DevBuf<int> tc_err;    // tensor-core operator: set when a bounded wait ran out
   bool tc_err_init = false;
+  int tc_win = 8;            // tensor-core operator: emitters per accumulator before it is drained
   bool pairs_ready = false;  // FP32 operator data (bucket plan or pair table) is built
 
   // volume lookup (particles at different heights): replaces the radial table when set; `kind`,
@@ -233,11 +236,13 @@ struct sg_context {
   // FP32 kernel autotuner: per RHS count, the fastest of the per-receiver, the bucketed and the
   // pair-symmetric kernel
   struct Tuned {
-    int nrhs, variant;  // 0 per-receiver, 1 bucketed, 2 pair-symmetric, 3 pair-symmetric (2 warps per receiver)
+    int nrhs, variant;  // 0 per-receiver, 1 bucketed, 2 pair-symmetric, 3 pair-symmetric (2 warps per receiver),
+                        // 4 tensor cores (3xTF32)
     int rt;             // per-receiver kernel: RHS tile per CTA
     float ms_receiver, ms_bucket;  // best per-receiver tile, bucketed (< 0: not a candidate)
     int sym_rt;         // pair-symmetric kernel: RHS tile per CTA
     float ms_sym;       // best pair-symmetric tile and layout (< 0: not a candidate)
+    float ms_tc;        // tensor-core operator (< 0: not a candidate)
   };
   std::vector<Tuned> tuned;
   std::vector<std::pair<int, int>> tuned_df;  // double-float kernel: (nrhs, RHS tile)

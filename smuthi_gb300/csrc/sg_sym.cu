@@ -640,11 +640,16 @@ int launch_sym_matvec(sg_context *c, const double2 *x, double2 *y, int R, bool m
     if (P == 1) launch_sym_r<4, 1>(c, L, rt, split, st);
     else launch_sym_r<4, 2>(c, L, rt, split, st);
   }
+  launch_fp32_epilogue(c, x, y, R, master, st);
+  return 3;  // conversion, coupling, epilogue (the memset is not a kernel of this library)
+}
+
+void launch_fp32_epilogue(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st) {
+  const size_t len = (size_t)c->n * c->bs * R;
   sym_epilogue_kernel<<<(unsigned)((len + 255) / 256), 256, 0, st>>>(c->sym_yacc.ptr, x, y, c->n, c->bs, R,
                                                                      master ? 1 : 0, c->tmat.ptr, c->ptype.ptr,
                                                                      c->t_diag);
   SG_CUDA(cudaGetLastError());
-  return 3;  // conversion, coupling, epilogue (the memset is not a kernel of this library)
 }
 
 // reads and clears the pair-symmetric kernel's error flag (synchronises the stream)

@@ -127,7 +127,8 @@ def main(argv=None):
     if a.volume:
         out["table_shape"] = system["table_shape"]
     if a.precision == "fp32" and not a.volume:
-        out["fp32_kernel"] = dict(zip(("variant", "rhs_tile", "ms_per_receiver", "ms_bucketed", "ms_symmetric"),
+        out["fp32_kernel"] = dict(zip(("variant", "rhs_tile", "ms_per_receiver", "ms_bucketed", "ms_symmetric",
+                                       "ms_tensor_core"),
                                       ctx.fp32_autotune(a.nrhs)))
     print(json.dumps(out))
     ctx.close()

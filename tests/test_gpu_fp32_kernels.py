@@ -123,8 +123,8 @@ def test_full_size_c2_symmetric_kernel(gpu_context):
                                             interpolator_kind="cubic", context=gpu_context)
     yt = gpu_context.coupling_matvec(X, _lib.SG_FP32)
     assert gc.relerr(yt, y64) < TOL32
-    variant, tile, ms_rec, ms_bucket, ms_sym = gpu_context.fp32_autotune(16)
-    assert variant in (0, 1, 2, 3) and ms_rec > 0 and ms_sym > 0
+    variant, tile, ms_rec, ms_bucket, ms_sym, ms_tc = gpu_context.fp32_autotune(16)
+    assert variant in (0, 1, 2, 3, 4) and ms_rec > 0 and ms_sym > 0 and ms_tc > 0
     del W2
 
 
