@@ -16,8 +16,9 @@
 //     e^{i (m2 - m1) phi} (powers computed per emitter by one lane each and exchanged by shuffles),
 //     split every value into a TF32 high part and an FP32 remainder and store the block into the
 //     stage in the canonical no-swizzle K-major layout (one 8 x 4 core tile per warp instruction,
-//     128 contiguous bytes, no bank conflicts); coefficient loads of up to four tiles are in flight
-//     per thread;
+//     128 contiguous bytes, no bank conflicts); coefficient loads of up to five tiles are in flight
+//     per thread, and the coefficient block of every receiver's pair three emitters ahead is pulled
+//     into L2 with one bulk prefetch;
 //   * one thread copies x_j's pre-split panel (hi | lo, contiguous) into the stage with one
 //     cp.async.bulk completing on the stage's mbarrier;
 //   * one thread issues the tcgen05.mma instructions (kind::tf32, M = 128, N = 2R, K = 8; hi*hi +
@@ -44,6 +45,7 @@ namespace sg {
 static constexpr int kTcProducers = 16;                   // producer warps
 static constexpr int kTcWarps = 6 + kTcProducers;         // 4 drain, 1 MMA, 1 copy, producers
 static constexpr int kTcThreads = 32 * kTcWarps;          // 704
+static constexpr int kTcPrefetch = 3;                     // emitters between an L2 prefetch and its use
 static constexpr long long kTcWaitCycles = 2000000000LL;  // ~1 s at 2 GHz per wait
 static constexpr unsigned kTcFull = 0xffffffffu;
 static constexpr int kTcSmemBudget = 227 * 1024;
@@ -77,14 +79,17 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
   return d;
 }
 
+// true when the phase of `parity` has completed. A thread whose phase is still open is suspended
+// until the phase completes or about 0.1 ms have passed (the suspend-time hint), so waiting roles
+// take no issue slots from the producers while they wait.
 __device__ __forceinline__ bool tc_poll(uint32_t bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
-      : "r"(bar), "r"(parity)
+      : "r"(bar), "r"(parity), "r"(100000u)
       : "memory");
   return ok != 0;
 }
@@ -158,7 +163,7 @@ struct TcShape {
   static constexpr int TPR = (BP / 8) * (BP / 4);      // 8 x 4 core tiles per receiver
   static constexpr int TILES = RPC * TPR;
   static constexpr int UNR = (TILES + kTcProducers - 1) / kTcProducers;
-  static constexpr int GRP = UNR < 4 ? UNR : 4;  // tiles whose loads are in flight together
+  static constexpr int GRP = UNR <= 5 ? UNR : 4;  // tiles whose loads are in flight together
   static constexpr int G = 32 / RPC;             // lanes per receiver in the phase exchange
   static constexpr int COLS = 3 * NN;            // two accumulators and the total
   static constexpr int NCOLS = COLS <= 32 ? 32 : (COLS <= 64 ? 64 : (COLS <= 128 ? 128 : (COLS <= 256 ? 256 : 512)));
@@ -224,12 +229,33 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
     const int grp = lane / Sh::G;  // receiver whose pair data and phase powers this lane holds
     const int gi = i0 + grp;
     const bool gvalid = grp < RPC && gi < N;
+    // Per-thread invariants of every tile this warp builds (the same for all emitters):
+    // coff = element offset n2 * bs + n1 within a coefficient plane (-1: padding or no receiver);
+    // sinfo = store offset tc_off(row, n2) (bits 0-15) | phase source lane r * G + |dm| (bits 16-20)
+    //         | conjugate flag dm < 0 (bit 21) | pair-data source lane r * G (bits 22-26).
+    int coff[Sh::UNR], sinfo[Sh::UNR];
+#pragma unroll
+    for (int u = 0; u < Sh::UNR; ++u) {
+      const int tile = p + kTcProducers * u;
+      const int r = (tile / Sh::TPR) % RPC, tr = tile % Sh::TPR;
+      const int n1 = (tr / (BP / 4)) * 8 + (lane & 7), n2 = (tr % (BP / 4)) * 4 + (lane >> 3);
+      const bool valid = tile < Sh::TILES && i0 + r < N && n1 < bs && n2 < bs;
+      const int dm = valid ? mofn_s[n2] - mofn_s[n1] : 0;
+      coff[u] = valid ? n2 * bs + n1 : -1;
+      sinfo[u] = tc_off<KC>(r * 2 * BP + n1, n2) | ((r * Sh::G + (dm < 0 ? -dm : dm)) << 16) | ((dm < 0 ? 1 : 0) << 21) |
+                 ((r * Sh::G) << 22);
+    }
+    const size_t plane = (size_t)bs2, block = (size_t)NC * bs2;
     int4 pd_next = gvalid ? __ldg(&a.pairs[(size_t)gi * N]) : make_int4(0, 0, 0x3f800000, 0);
     for (int jj = 0; jj < N; ++jj) {
       if (__shfl_sync(kTcFull, *abort_flag, 0)) break;  // one verdict per warp
       const int s = jj % S, q = jj / S;
       const int4 pd = pd_next;
       if (jj + 1 < N && gvalid) pd_next = __ldg(&a.pairs[(size_t)gi * N + jj + 1]);
+      // producer warp 0, lane r < RPC: interval of receiver r at emitter jj + kTcPrefetch, whose
+      // coefficient block (contiguous) is pulled into L2 at the end of this iteration
+      const bool pf = p == 0 && lane < RPC && i0 + lane < N && jj + kTcPrefetch < N;
+      const int kpf = pf ? __ldg(&a.pairs[(size_t)(i0 + lane) * N + jj + kTcPrefetch].x) : 0;
       // phase power e^{i d phi}, d = this lane's index within its receiver group (<= dmax)
       float pr = 1.f, pim = 0.f;
       {
@@ -241,25 +267,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
           pr = nr;
         }
       }
-      float *Ah = stages + (size_t)s * Sh::STAGE, *Al = Ah + Sh::ATILE;
+      float *Ah = stages + (size_t)s * Sh::STAGE;
       bool waited = (q == 0);
 #pragma unroll
       for (int g0 = 0; g0 < Sh::UNR; g0 += Sh::GRP) {
         float2 cf[Sh::GRP][NC];
         float tt[Sh::GRP];
-        bool live[Sh::GRP];
 #pragma unroll
         for (int u = 0; u < Sh::GRP; ++u) {
-          const int tile = p + kTcProducers * (g0 + u);
-          const int r = (tile / Sh::TPR) % RPC, tr = tile % Sh::TPR;
-          const int n1 = (tr / (BP / 4)) * 8 + (lane & 7), n2 = (tr % (BP / 4)) * 4 + (lane >> 3);
-          const int k = __shfl_sync(kTcFull, pd.x, r * Sh::G);
-          tt[u] = __shfl_sync(kTcFull, __int_as_float(pd.y), r * Sh::G);
-          live[u] = (g0 + u < Sh::UNR) && tile < Sh::TILES && i0 + r < N && n1 < bs && n2 < bs;
-          const float2 *cp = a.coef + ((size_t)k * NC * bs2 + (size_t)n2 * bs + n1);
+          if (g0 + u >= Sh::UNR) continue;
+          const int ks = (sinfo[g0 + u] >> 22) & 31;
+          const int k = __shfl_sync(kTcFull, pd.x, ks);
+          tt[u] = __shfl_sync(kTcFull, __int_as_float(pd.y), ks);
+          const int off = coff[g0 + u];
+          const float2 *cp = a.coef + ((size_t)k * block + (off < 0 ? 0 : off));
 #pragma unroll
-          for (int ci = 0; ci < NC; ++ci)
-            cf[u][ci] = live[u] ? __ldg(cp + (size_t)ci * bs2) : make_float2(0.f, 0.f);
+          for (int ci = 0; ci < NC; ++ci) cf[u][ci] = off >= 0 ? __ldg(cp + ci * plane) : make_float2(0.f, 0.f);
         }
         if (!waited) {
           if (!tc_waitw(smem_u32(&empty[s]), (uint32_t)((q - 1) & 1))) {
@@ -273,16 +296,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
         }
 #pragma unroll
         for (int u = 0; u < Sh::GRP; ++u) {
-          const int tile = p + kTcProducers * (g0 + u);
-          if (g0 + u >= Sh::UNR || tile >= Sh::TILES) continue;  // warp-uniform
-          const int r = tile / Sh::TPR, tr = tile % Sh::TPR;
-          const int n1 = (tr / (BP / 4)) * 8 + (lane & 7), n2 = (tr % (BP / 4)) * 4 + (lane >> 3);
-          const int dm = mofn_s[n2] - mofn_s[n1];
-          const int src = r * Sh::G + (dm < 0 ? -dm : dm);
+          if (g0 + u >= Sh::UNR || p + kTcProducers * (g0 + u) >= Sh::TILES) continue;  // warp-uniform
+          const int si = sinfo[g0 + u];
+          const int src = (si >> 16) & 31;
           const float er = __shfl_sync(kTcFull, pr, src);
           float ei = __shfl_sync(kTcFull, pim, src);
-          if (dm < 0) ei = -ei;
-          if (i0 + r >= N || n1 >= bs || n2 >= bs) continue;  // padding stays zero
+          if (si & (1 << 21)) ei = -ei;
+          if (coff[g0 + u] < 0) continue;  // padding stays zero
           float lr = cf[u][NC - 1].x, li = cf[u][NC - 1].y;
 #pragma unroll
           for (int ci = NC - 2; ci >= 0; --ci) {
@@ -292,17 +312,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
           // the self pair (rho = 0) is not zero: it is the particle's coupling to itself through the layers
           const float wr = lr * er - li * ei, wi = lr * ei + li * er;
           const float wrh = tf32_hi(wr), wih = tf32_hi(wi);
-          const int row = r * 2 * BP + n1;
-          Ah[tc_off<KC>(row, n2)] = wrh;
-          Al[tc_off<KC>(row, n2)] = wr - wrh;
-          Ah[tc_off<KC>(row + BP, n2)] = wih;
-          Al[tc_off<KC>(row + BP, n2)] = wi - wih;
+          float *dst = Ah + (si & 0xFFFF);  // Re W in row n1, Im W in row BP + n1 (BP * BP floats further)
+          dst[0] = wrh;
+          dst[Sh::ATILE] = wr - wrh;
+          dst[BP * BP] = wih;
+          dst[Sh::ATILE + BP * BP] = wi - wih;
         }
       }
       if (!waited) break;  // the wait above ran out
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
       if (lane == 0) tc_arrive(smem_u32(&full_a[s]));
+      if (pf)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a.coef + (size_t)kpf * NC * bs2),
+                     "r"((uint32_t)(NC * bs2 * sizeof(float2)))
+                     : "memory");
     }
   } else if (warp == 5) {
     // ------------------------------------------------------------------ x panel copies

@@ -95,7 +95,8 @@ def main(argv=None):
     ap.add_argument("--nearfield", type=int, default=0, metavar="POINTS",
                     help="time the near field of a plane-wave expansion at this many points instead")
     ap.add_argument("--fp32-kernel", default=None, metavar="VARIANT:TILE",
-                    help="fix the FP32 kernel (0 per-receiver, 1 bucketed, 2 pair-symmetric) and its RHS tile "
+                    help="fix the FP32 kernel (0 per-receiver, 1 bucketed, 2 pair-symmetric, 3 pair-symmetric "
+                         "with two warps per receiver, 4 tensor cores with tile = nrhs) and its RHS tile "
                          "instead of the autotuner's choice")
     a = ap.parse_args(argv)
     if a.nearfield:

@@ -3,7 +3,8 @@
 The FP32 operator drives the correction solves of the mixed-precision refinement; the autotuner
 picks among the per-receiver kernel (RHS tiles 1-16), the interval-bucketed kernel and the
 pair-symmetric kernel (one interpolation per unordered pair for both directions, with one or two warps
-per receiver). Each is fixed
+per receiver). The tensor-core operator (variant 4: tcgen05 3xTF32 with drained
+accumulators) is held to the same bound. Each is fixed
 here with ``fp32_set_kernel`` and compared, through the C ABI, with the FP64 operator (relative
 2-norm 2e-5, the FP32 bound the other FP32 tests use) and with the reference's W x / M x.
 Also: the full (non-diagonal) T-matrix epilogue of the FP64, per-receiver FP32 and pair-symmetric
@@ -25,6 +26,8 @@ def _variants(ctx, R, bs):
     out = [(0, t) for t in (1, 2, 4, 8, 16) if R % t == 0]
     out += [(2, t) for t in (1, 2, 4, 8, 16) if R % t == 0 and t <= (16 if bs <= 32 else 8)]
     out += [(3, t) for t in (4, 8, 16) if R % t == 0 and t <= (16 if bs <= 32 else 8)]
+    if R in (16, 32, 64) and bs <= 48:
+        out.append((4, R))
     return out
 
 
@@ -45,7 +48,7 @@ def test_fp32_kernels_match_fp64_and_reference(name, gpu_context):
         parts, ls, wl, W, M = _product_system(g, kind, gpu_context)
         bs = int(max((p.l_max * (p.l_max + 2) * 2) for p in parts))  # upper bound of the padded blocksize
         x = g["x_" + kind]
-        for R in (1, 3, 16):
+        for R in (1, 3, 16, 64):
             X = _rhs(x, R, 7)
             y64 = gpu_context.coupling_matvec(X, _lib.SG_FP64)
             m64 = gpu_context.master_matvec(X, _lib.SG_FP64)
@@ -72,13 +75,13 @@ def test_full_t_epilogue(name, gpu_context):
     blocks = 0.05 * (rng.standard_normal((2, bs, bs)) + 1j * rng.standard_normal((2, bs, bs)))
     types = (np.arange(n) % 2).astype(np.int32)
     gpu_context.set_tmatrix(blocks, types, diagonal=False)
-    for R in (1, 4):
+    for R in (1, 4, 16):
         X = _rhs(g["x_" + kind], R, 3)
         Xr = X.reshape(n, bs, R)
         wx = gpu_context.coupling_matvec(X, _lib.SG_FP64).reshape(n, bs, R)
         ref = (Xr - np.einsum("iab,ibr->iar", blocks[types], wx)).reshape(X.shape)
         assert gc.relerr(gpu_context.master_matvec(X, _lib.SG_FP64), ref) < 1e-13
-        for v, t in [(0, 1), (2, 1)] + ([(0, 4), (2, 4), (3, 4)] if R == 4 else []):
+        for v, t in [(0, 1), (2, 1)] + ([(0, 4), (2, 4), (3, 4)] if R == 4 else []) + ([(4, 16)] if R == 16 else []):
             gpu_context.fp32_set_kernel(R, v, t)
             assert gc.relerr(gpu_context.master_matvec(X, _lib.SG_FP32), ref) < TOL32, (R, v, t)
 
@@ -87,7 +90,7 @@ def test_fp32_set_kernel_rejects_bad_choices(gpu_context):
     from smuthi_gb300 import _lib
     g = gc.load("c1")
     _product_system(g, "linear", gpu_context)
-    for args in [(16, 0, 3), (4, 0, 8), (16, 2, 32), (6, 2, 4), (4, 5, 1), (2, 3, 2)]:
+    for args in [(16, 0, 3), (4, 0, 8), (16, 2, 32), (6, 2, 4), (4, 5, 1), (2, 3, 2), (8, 4, 8), (16, 4, 8)]:
         with pytest.raises(_lib.SmuthiGB300Error) as e:
             gpu_context.fp32_set_kernel(*args)
         assert e.value.code == _lib.SG_ERR_ARG
@@ -130,12 +133,14 @@ def test_full_size_c2_symmetric_kernel(gpu_context):
 
 def test_full_size_c3_operator_and_mixed_solve(gpu_context):
     """5000 spheres, blocksize 48, cubic lookup at 2 nm (the mixed-precision shape at full size): FP64
-    operator rows against the oracle, every FP32 kernel against FP64, and the chosen form's solve of
-    four plane waves to an FP64-true relative residual of 1e-6."""
+    operator rows against the oracle, every FP32 kernel against FP64 at 4 RHS, the tensor-core operator
+    against the double-float operator at 64 RHS (bound 5e-6), and the chosen form's solve of 64 plane
+    waves (the 64-wave batch of this shape) to an FP64-grade relative residual of 1e-6, re-checked with
+    the FP64 operator on four of the waves."""
     import oracle.physics as ophys
     import oracle.solve as osv
     from smuthi_gb300 import _lib, learned
-    system = learned.film_system("c3", nrhs=4, ctx=gpu_context)
+    system = learned.film_system("c3", nrhs=64, ctx=gpu_context)
     W, n, bs = system["W"], system["n"], system["blocksize"]
     assert (n, bs) == (5000, 48)
     rng = np.random.default_rng(13)
@@ -147,11 +152,15 @@ def test_full_size_c3_operator_and_mixed_solve(gpu_context):
     yo = Wo.matvec(x, rows=rows)
     sel = np.concatenate([np.arange(r * bs, (r + 1) * bs) for r in rows])
     assert gc.relerr(y[sel], yo[sel]) < 1e-11
-    X = np.ascontiguousarray(system["rhs"])
-    y64 = gpu_context.coupling_matvec(X, _lib.SG_FP64)
+    B = np.ascontiguousarray(system["rhs"])
+    X4 = np.ascontiguousarray(B[:, :4])
+    y64 = gpu_context.coupling_matvec(X4, _lib.SG_FP64)
     for v, t in [(0, 4), (2, 4), (3, 4)]:
         gpu_context.fp32_set_kernel(4, v, t)
-        assert gc.relerr(gpu_context.coupling_matvec(X, _lib.SG_FP32), y64) < TOL32, (v, t)
-    sol, info = gpu_context.gmres(X, np.zeros_like(X), 1e-6, restart=64, precision=_lib.SG_FP32 | _lib.SG_DF64)
-    assert info.converged == 4
-    assert gpu_context.true_residual(X, sol).max() <= 1e-6
+        assert gc.relerr(gpu_context.coupling_matvec(X4, _lib.SG_FP32), y64) < TOL32, (v, t)
+    ydf = gpu_context.coupling_matvec(B, _lib.SG_DF64)
+    assert gc.relerr(ydf[:, :4], y64) < 1e-12
+    assert gc.relerr(gpu_context.coupling_matvec(B, _lib.SG_TF32X3), ydf) < 5e-6
+    sol, info = gpu_context.gmres(B, np.zeros_like(B), 1e-6, restart=64, precision=_lib.SG_FP32 | _lib.SG_DF64)
+    assert info.converged == 64
+    assert gpu_context.true_residual(X4, np.ascontiguousarray(sol[:, :4])).max() <= 1e-6

@@ -277,22 +277,21 @@ def test_mixed_solution_with_df64_residuals(name, gpu_context):
 
 @pytest.mark.parametrize("name", ["c5s", "c2s", "c1"])
 def test_tensor_core_operator_matches_fp64(name, gpu_context):
-    """The tcgen05 3xTF32 operator stays within 1e-5 of the FP64 operator on these sizes (<= 120
-    emitters). Its error grows with the number of emitters: the tensor core's accumulation into
-    tensor memory is not round-to-nearest FP32, which is why the FP32 kernel stays the default."""
+    """The tcgen05 3xTF32 operator (accumulators drained every 8 emitters into an FP32 total) within
+    5e-6 of the FP64 operator for 16, 32 and 64 right-hand sides, with the self pairs included."""
     from smuthi_gb300 import _lib
     g = gc.load(name)
     kind = _kinds(g)[0]
     parts, ls, wl, W, M = _product_system(g, kind, gpu_context)
     x = g["x_" + kind]
     rng = np.random.default_rng(4)
-    for R in (8, 16, 32):
+    for R in (16, 32, 64):
         X = np.ascontiguousarray(np.stack([x * np.exp(2j * np.pi * rng.random()) * (1 + 0.5 * rng.random())
                                            for _ in range(R)], axis=1))
         for fn in (gpu_context.coupling_matvec, gpu_context.master_matvec):
             ref = fn(X, _lib.SG_FP64)
             tc = fn(X, _lib.SG_TF32X3)
-            assert gc.relerr(tc, ref) < 1e-5, (R, fn.__name__, gc.relerr(tc, ref))
+            assert gc.relerr(tc, ref) < 5e-6, (R, fn.__name__, gc.relerr(tc, ref))
 
 
 @pytest.mark.parametrize("count", [1, 2])
