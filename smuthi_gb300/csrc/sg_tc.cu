@@ -12,13 +12,12 @@
 // that all CTAs read the same x_j panels at about the same time (one DRAM read per panel per wave
 // of CTAs). The CTA is warp-specialised and pipelined over S shared-memory stages:
 //
-//   * 16 producer warps interpolate the interval's coefficients (FP32 Horner), fold in the phase
+//   * 16 or 24 producer warps (two to four 8 x 4 tiles each) interpolate the interval's coefficients (FP32 Horner), fold in the phase
 //     e^{i (m2 - m1) phi} (powers computed per emitter by one lane each and exchanged by shuffles),
 //     split every value into a TF32 high part and an FP32 remainder and store the block into the
 //     stage in the canonical no-swizzle K-major layout (one 8 x 4 core tile per warp instruction,
-//     128 contiguous bytes, no bank conflicts); coefficient loads of up to five tiles are in flight
-//     per thread, and the coefficient block of every receiver's pair three emitters ahead is pulled
-//     into L2 with one bulk prefetch;
+//     128 contiguous bytes, no bank conflicts); the coefficient loads of all tiles of a thread are
+//     in flight together;
 //   * one thread copies x_j's pre-split panel (hi | lo, contiguous) into the stage with one
 //     cp.async.bulk completing on the stage's mbarrier;
 //   * one thread issues the tcgen05.mma instructions (kind::tf32, M = 128, N = 2R, K = 8; hi*hi +
@@ -42,10 +41,7 @@
 
 namespace sg {
 
-static constexpr int kTcProducers = 16;                   // producer warps
-static constexpr int kTcWarps = 6 + kTcProducers;         // 4 drain, 1 MMA, 1 copy, producers
-static constexpr int kTcThreads = 32 * kTcWarps;          // 704
-static constexpr int kTcPrefetch = 3;                     // emitters between an L2 prefetch and its use
+static constexpr int kTcRoles = 6;                        // 4 drain warps, 1 MMA warp, 1 copy warp
 static constexpr long long kTcWaitCycles = 2000000000LL;  // ~1 s at 2 GHz per wait
 static constexpr unsigned kTcFull = 0xffffffffu;
 static constexpr int kTcSmemBudget = 227 * 1024;
@@ -162,8 +158,12 @@ struct TcShape {
   static constexpr int S = S0 > 4 ? 4 : S0;            // pipeline stages
   static constexpr int TPR = (BP / 8) * (BP / 4);      // 8 x 4 core tiles per receiver
   static constexpr int TILES = RPC * TPR;
-  static constexpr int UNR = (TILES + kTcProducers - 1) / kTcProducers;
-  static constexpr int GRP = UNR <= 5 ? UNR : 4;  // tiles whose loads are in flight together
+  // producer warps: three 8 x 4 tiles each at BP = 48 (30 warps), four at BP = 32, two at BP = 16;
+  // more warps hide more of the coefficient stream's latency (960 threads is the largest multiple)
+  static constexpr int NPROD = TILES % 24 == 0 ? 24 : 16;
+  static constexpr int THREADS = 32 * (kTcRoles + NPROD);
+  static constexpr int UNR = (TILES + NPROD - 1) / NPROD;
+  static constexpr int GRP = UNR < 4 ? UNR : 4;  // tiles whose loads are in flight together
   static constexpr int G = 32 / RPC;             // lanes per receiver in the phase exchange
   static constexpr int COLS = 3 * NN;            // two accumulators and the total
   static constexpr int NCOLS = COLS <= 32 ? 32 : (COLS <= 64 ? 64 : (COLS <= 128 ? 128 : (COLS <= 256 ? 256 : 512)));
@@ -175,8 +175,9 @@ struct TcShape {
 };
 
 template <int NC, int BP, int R>
-__global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs a) {
+__global__ void __launch_bounds__(TcShape<BP, R>::THREADS, 1) tc_coupling_kernel(const TcArgs a) {
   using Sh = TcShape<BP, R>;
+  constexpr int kTcThreads = Sh::THREADS, kTcProducers = Sh::NPROD;
   constexpr int NN = Sh::NN, RPC = Sh::RPC, KC = Sh::KC, S = Sh::S;
   extern __shared__ __align__(1024) unsigned char tc_smem[];
   float *stages = reinterpret_cast<float *>(tc_smem);
@@ -223,9 +224,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  if (warp >= 6) {
+  if (warp >= kTcRoles) {
     // ------------------------------------------------------------------ producers
-    const int p = warp - 6;
+    const int p = warp - kTcRoles;
     const int grp = lane / Sh::G;  // receiver whose pair data and phase powers this lane holds
     const int gi = i0 + grp;
     const bool gvalid = grp < RPC && gi < N;
@@ -252,10 +253,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
       const int s = jj % S, q = jj / S;
       const int4 pd = pd_next;
       if (jj + 1 < N && gvalid) pd_next = __ldg(&a.pairs[(size_t)gi * N + jj + 1]);
-      // producer warp 0, lane r < RPC: interval of receiver r at emitter jj + kTcPrefetch, whose
-      // coefficient block (contiguous) is pulled into L2 at the end of this iteration
-      const bool pf = p == 0 && lane < RPC && i0 + lane < N && jj + kTcPrefetch < N;
-      const int kpf = pf ? __ldg(&a.pairs[(size_t)(i0 + lane) * N + jj + kTcPrefetch].x) : 0;
       // phase power e^{i d phi}, d = this lane's index within its receiver group (<= dmax)
       float pr = 1.f, pim = 0.f;
       {
@@ -323,10 +320,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_coupling_kernel(const TcArgs
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
       if (lane == 0) tc_arrive(smem_u32(&full_a[s]));
-      if (pf)
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a.coef + (size_t)kpf * NC * bs2),
-                     "r"((uint32_t)(NC * bs2 * sizeof(float2)))
-                     : "memory");
     }
   } else if (warp == 5) {
     // ------------------------------------------------------------------ x panel copies
@@ -522,7 +515,7 @@ static void tc_launch_t(const TcArgs &a, cudaStream_t st) {
     SG_CUDA(cudaFuncSetAttribute(tc_coupling_kernel<NC, BP, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)Sh::smem()));
   const unsigned grid = (unsigned)((a.n + Sh::RPC - 1) / Sh::RPC);
-  tc_coupling_kernel<NC, BP, R><<<grid, kTcThreads, Sh::smem(), st>>>(a);
+  tc_coupling_kernel<NC, BP, R><<<grid, Sh::THREADS, Sh::smem(), st>>>(a);
   SG_CUDA(cudaGetLastError());
 }
 
