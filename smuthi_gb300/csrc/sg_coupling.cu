@@ -186,9 +186,19 @@ __global__ void __launch_bounds__(kThreads) coupling_kernel(const CouplingLaunch
           u.x = ph_re[q] * xr - ph_im[q] * xim;
           u.y = ph_re[q] * xim + ph_im[q] * xr;
           // FP64: [r][n2] (lane-consecutive writes); FP32: [n2][r] (the n2 loop reads the RHS tile
-          // with vector loads, which matters more than the write conflicts)
-          if (sizeof(Real) == sizeof(double)) ubuf[r * bs + nrow[q]] = u;
-          else ubuf[nrow[q] * RT + r] = u;
+          // with vector loads, which matters more than the write conflicts); double-float with an
+          // even tile: [n2][RHS pair][re.hi x2, re.lo x2, im.hi x2, im.lo x2] for the packed path
+          if constexpr (std::is_same<Real, df64>::value && RT % 2 == 0) {
+            float *f = reinterpret_cast<float *>(ubuf) + ((size_t)nrow[q] * (RT / 2) + r / 2) * 8 + (r & 1);
+            f[0] = u.x.hi;
+            f[2] = u.x.lo;
+            f[4] = u.y.hi;
+            f[6] = u.y.lo;
+          } else if (sizeof(Real) == sizeof(double)) {
+            ubuf[r * bs + nrow[q]] = u;
+          } else {
+            ubuf[nrow[q] * RT + r] = u;
+          }
         }
       }
     }
@@ -224,6 +234,67 @@ __global__ void __launch_bounds__(kThreads) coupling_kernel(const CouplingLaunch
           }
         }
       }
+    } else if constexpr (std::is_same<Real, df64>::value && RT % 2 == 0) {
+      // double-float, RHS in pairs on the packed FP32x2 instructions (fma_p: the scalar operations
+      // on two values at once); coefficients of the next column are fetched while this one is applied
+      df64p pp_re[P][RT / 2], pp_im[P][RT / 2];
+#pragma unroll
+      for (int q = 0; q < P; ++q)
+#pragma unroll
+        for (int h = 0; h < RT / 2; ++h) {
+          pp_re[q][h].hi = pp_re[q][h].lo = pp_im[q][h].hi = pp_im[q][h].lo = make_float2(0.f, 0.f);
+        }
+      cplx cf[P][NC];
+#pragma unroll
+      for (int q = 0; q < P; ++q)
+#pragma unroll
+        for (int ci = 0; ci < NC; ++ci) cf[q][ci] = ldc(cbase + ci * bs2 + nrowc[q]);
+      const float4 *ub = reinterpret_cast<const float4 *>(ubuf);
+      for (int n2 = 0; n2 < bs; ++n2) {
+        const int n2n = n2 + 1 < bs ? n2 + 1 : n2;
+        cplx nf[P][NC];
+#pragma unroll
+        for (int q = 0; q < P; ++q)
+#pragma unroll
+          for (int ci = 0; ci < NC; ++ci) nf[q][ci] = ldc(cbase + ci * bs2 + (size_t)n2n * bs + nrowc[q]);
+        df64p ure[RT / 2], uim[RT / 2];
+#pragma unroll
+        for (int h = 0; h < RT / 2; ++h) {
+          const float4 a0 = ub[((size_t)n2 * (RT / 2) + h) * 2], a1 = ub[((size_t)n2 * (RT / 2) + h) * 2 + 1];
+          ure[h].hi = make_float2(a0.x, a0.y);
+          ure[h].lo = make_float2(a0.z, a0.w);
+          uim[h].hi = make_float2(a1.x, a1.y);
+          uim[h].lo = make_float2(a1.z, a1.w);
+        }
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+          Real lr = cf[q][NC - 1].x, li = cf[q][NC - 1].y;
+#pragma unroll
+          for (int ci = NC - 2; ci >= 0; --ci) {
+            lr = fma(lr, t, cf[q][ci].x);
+            li = fma(li, t, cf[q][ci].y);
+          }
+          const df64b blr = dfw::df_bcast(lr), bli = dfw::df_bcast(li), bnli = dfw::df_bcast(-li);
+#pragma unroll
+          for (int h = 0; h < RT / 2; ++h) {
+            pp_re[q][h] = dfw::fma_p(blr, ure[h], pp_re[q][h]);
+            pp_re[q][h] = dfw::fma_p(bnli, uim[h], pp_re[q][h]);
+            pp_im[q][h] = dfw::fma_p(blr, uim[h], pp_im[q][h]);
+            pp_im[q][h] = dfw::fma_p(bli, ure[h], pp_im[q][h]);
+          }
+#pragma unroll
+          for (int ci = 0; ci < NC; ++ci) cf[q][ci] = nf[q][ci];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < P; ++q)
+#pragma unroll
+        for (int h = 0; h < RT / 2; ++h) {
+          pa_re[q][2 * h] = df64(pp_re[q][h].hi.x, pp_re[q][h].lo.x);
+          pa_re[q][2 * h + 1] = df64(pp_re[q][h].hi.y, pp_re[q][h].lo.y);
+          pa_im[q][2 * h] = df64(pp_im[q][h].hi.x, pp_im[q][h].lo.x);
+          pa_im[q][2 * h + 1] = df64(pp_im[q][h].hi.y, pp_im[q][h].lo.y);
+        }
     } else {
       // FP32 and double-float: the coefficient loads are L2-latency bound, so the next column's
       // coefficients are fetched into registers while the current column is applied (the last

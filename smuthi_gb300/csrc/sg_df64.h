@@ -85,6 +85,76 @@ __device__ __forceinline__ df64 fma(df64 a, df64 b, df64 c) {
   return df64(s.hi, s.lo + (c.lo + e));
 }
 
+// ---- two double-float values at once on the packed FP32x2 instructions (sm_100 and later)
+__device__ __forceinline__ float2 f2_add(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 f2_sub(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 f2_mul(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+
+// two double-float values: (hi.x, lo.x) and (hi.y, lo.y)
+struct df64p {
+  float2 hi, lo;
+};
+
+// a double-float multiplier broadcast to both lanes, with its negated high word
+struct df64b {
+  float2 hi, lo, nhi;
+};
+
+__device__ __forceinline__ df64b df_bcast(df64 a) {
+  df64b r;
+  r.hi = make_float2(a.hi, a.hi);
+  r.lo = make_float2(a.lo, a.lo);
+  r.nhi = make_float2(-a.hi, -a.hi);
+  return r;
+}
+
+// fma(a, b, c) above on two values at once, with the same operations in the same order, so each
+// lane's result equals the scalar one bit for bit: the product's negation np = -p is exact, so
+// fma(a.hi, b.hi, -p) = fma(a.hi, b.hi, np), c.hi + p = c.hi - np and p - bb = -(np + bb).
+__device__ __forceinline__ df64p fma_p(const df64b &a, df64p b, df64p c) {
+  const float2 np = f2_mul(a.nhi, b.hi);
+  float2 e = f2_fma(a.hi, b.hi, np);
+  e = f2_fma(a.hi, b.lo, e);
+  e = f2_fma(a.lo, b.hi, e);
+  const float2 s = f2_sub(c.hi, np);
+  const float2 bb = f2_sub(s, c.hi);
+  const float2 err = f2_sub(f2_sub(c.hi, f2_sub(s, bb)), f2_add(np, bb));
+  df64p r;
+  r.hi = s;
+  r.lo = f2_add(err, f2_add(c.lo, e));
+  return r;
+}
+
 // FP64 complex -> df64 complex (hi = nearest float, lo = nearest float of the remainder)
 __device__ __forceinline__ df64x2 df_from_double2(double2 v) {
   df64x2 r;
@@ -95,6 +165,8 @@ __device__ __forceinline__ df64x2 df_from_double2(double2 v) {
 
 }  // namespace dfw
 using dfw::df64;
+using dfw::df64b;
+using dfw::df64p;
 using dfw::df64x2;
 using dfw::df_from_double2;
 }  // namespace sg
