@@ -260,7 +260,8 @@ def run_ours(args, rank, world, local_rank):
                 1: "bucket_kernel (interval-bucketed)",
                 2: "sym_kernel (pair-symmetric, one warp per receiver, RHS tile %d)" % t32,
                 3: "sym_kernel (pair-symmetric, two warps per receiver, RHS tile %d)" % t32,
-                4: "tc_coupling_kernel (tcgen05 3xTF32, %d RHS)" % t32}.get(v32, "FP32 operator")
+                4: "tc_coupling_kernel (tcgen05 3xTF32, %d RHS)" % t32,
+                5: "tcsym_kernel (pair-symmetric tcgen05 3xTF32, %d RHS)" % t32}.get(v32, "FP32 operator")
         peak, bound = peak32, "fp32"
         byts = algorithmic_bytes(n, bs, kind, n_int, R, True)
     elif msdf >= ms64:
@@ -328,10 +329,11 @@ def run_ours(args, rank, world, local_rank):
                         "residual_arithmetic": args.residual,
                         "batched": True, "x0": "0",
                         "fp32_kernel": dict(zip(("variant", "rhs_tile", "ms_per_receiver", "ms_bucketed", "ms_symmetric",
-                                                 "ms_tensor_core"), ctx.fp32_autotune(R))),
+                                                 "ms_tensor_core", "ms_tensor_core_symmetric"), ctx.fp32_autotune(R))),
                         "fp32_kernel_variants": "0 = per-receiver, 1 = interval-bucketed, 2 = pair-symmetric (one warp per "
                                                 "receiver), 3 = pair-symmetric (two warps per receiver), 4 = tensor "
-                                                "cores (tcgen05 3xTF32); RHS tile autotuned"},
+                                                "cores (tcgen05 3xTF32), 5 = pair-symmetric tensor cores; RHS tile "
+                                                "autotuned"},
         "prep_s": round(prep_s, 2),
         "e2e": {"value": round(e2e_value, 6), "unit": UNIT, "h2d_bytes_per_step": int(2 * rhs.nbytes),
                 "d2h_bytes_per_step": int(rhs.nbytes)},
@@ -425,7 +427,8 @@ def run_target(args, local_rank):
                            "max_rel_residual_fp64": float(relres.max()), "learned_preconditioner": pname,
                            "precond_fallbacks": info.precond_fallbacks, "residual_arithmetic": "df64",
                            "fp32_kernel": dict(zip(("variant", "rhs_tile", "ms_per_receiver", "ms_bucketed",
-                                                    "ms_symmetric", "ms_tensor_core"), ctx.fp32_autotune(R)))},
+                                                    "ms_symmetric", "ms_tensor_core", "ms_tensor_core_symmetric"),
+                                                   ctx.fp32_autotune(R)))},
            "plain_fp64": {"s_per_rhs": round(plain_s, 3), "iterations": pinfo.iterations,
                           "fp64_matvecs": pinfo.fp64_matvecs, "rel_residual_fp64": float(prelres[0]),
                           "restart": 20, "x0": "b"},

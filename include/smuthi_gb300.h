@@ -172,21 +172,24 @@ int sg_launch_count(sg_context *ctx, int64_t *count);
 /* FP32-operator autotuner result for an RHS count: variant 0 = per-receiver kernel, 1 =
  * interval-bucketed kernel, 2 = pair-symmetric kernel (one interpolation per unordered pair serves
  * both directions; one warp per receiver), 3 = the pair-symmetric kernel with two warps per receiver
- * (each half of the RHS tile), 4 = the tensor-core operator (SG_TF32X3), -1 = not tuned yet;
- * rhs_tile = the chosen kernel's RHS tile per CTA (nrhs for variant 4); with the CUDA-event times
- * (ms) of one run of the best per-receiver tile, of the bucketed kernel, of the best pair-symmetric
- * tile and of the tensor-core operator (-1 when not a candidate; any output pointer may be NULL).
+ * (each half of the RHS tile), 4 = the tensor-core operator (SG_TF32X3), 5 = the pair-symmetric
+ * tensor-core operator (one interpolated block per unordered pair on tcgen05; blocksize <= 32 and
+ * 16 or 32 RHS), -1 = not tuned yet; rhs_tile = the chosen kernel's RHS tile per CTA (nrhs for
+ * variants 4 and 5); with the CUDA-event times (ms) of one run of the best per-receiver tile, of the
+ * bucketed kernel, of the best pair-symmetric tile and of the two tensor-core operators (-1 when not
+ * a candidate; any output pointer may be NULL).
  * The first FP32 application for a new RHS count times every candidate on the live operands
  * (synchronising the stream) and keeps the fastest. No counterpart in the reference. */
 int sg_fp32_autotune(sg_context *ctx, int nrhs, int *variant, int *rhs_tile, double *ms_receiver,
-                     double *ms_bucket, double *ms_symmetric, double *ms_tensor);
+                     double *ms_bucket, double *ms_symmetric, double *ms_tensor, double *ms_tensor_symmetric);
 
 /* Fixes the FP32 operator for an RHS count instead of timing the candidates: variant 0 =
  * per-receiver kernel (rhs_tile 1, 2, 4, 8 or 16 dividing nrhs), 1 = interval-bucketed kernel
  * (rhs_tile ignored; needs its plan), 2 = pair-symmetric kernel (rhs_tile a power of two dividing
  * nrhs, at most 16 for blocksize <= 32 and 8 for blocksize <= 64), 3 = pair-symmetric kernel with two
  * warps per receiver (the same tiles, at least 4), 4 = tensor-core operator (rhs_tile = nrhs, in
- * {16, 32, 64}; blocksize <= 48). Replaces an earlier choice for
+ * {16, 32, 64}; blocksize <= 48), 5 = pair-symmetric tensor-core operator (rhs_tile = nrhs, in
+ * {16, 32}; blocksize <= 32). Replaces an earlier choice for
  * that RHS count; set_particles / set_lookup clear it. For tests and measurements of one kernel; no
  * counterpart in the reference. */
 int sg_fp32_set_kernel(sg_context *ctx, int nrhs, int variant, int rhs_tile);

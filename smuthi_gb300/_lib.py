@@ -88,7 +88,7 @@ def _declare(L):
         "sg_launch_count": [_P, ctypes.POINTER(ctypes.c_int64)],
         "sg_measure_fma_peak": [_P, _I, ctypes.POINTER(_D)],
         "sg_fp32_autotune": [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D),
-                             ctypes.POINTER(_D), ctypes.POINTER(_D)],
+                             ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D)],
         "sg_fp32_set_kernel": [_P, _I, _I, _I],
         "sg_tc_set_window": [_P, _I],
         "sg_coupling_matvec_linear_noalloc": [_I, _I, _P, _I, _P, _I, _D, _D, _P, _P, _P, _I, _P],
@@ -259,19 +259,19 @@ class Context:
 
     def fp32_autotune(self, nrhs):
         """(variant, RHS tile, ms best per-receiver tile, ms bucketed, ms best pair-symmetric tile, ms tensor
-        cores) for an RHS count; variant -1 if not tuned yet (0 per-receiver, 1 bucketed, 2 pair-symmetric,
-        3 pair-symmetric with two warps per receiver, 4 tensor cores), a time is -1 when that kernel is not a
-        candidate."""
+        cores, ms pair-symmetric tensor cores) for an RHS count; variant -1 if not tuned yet (0 per-receiver,
+        1 bucketed, 2 pair-symmetric, 3 pair-symmetric with two warps per receiver, 4 tensor cores,
+        5 pair-symmetric tensor cores), a time is -1 when that kernel is not a candidate."""
         v = ctypes.c_int()
         t = ctypes.c_int()
-        ms = [ctypes.c_double() for _ in range(4)]
+        ms = [ctypes.c_double() for _ in range(5)]
         check(lib().sg_fp32_autotune(self.h, int(nrhs), ctypes.byref(v), ctypes.byref(t),
                                      *[ctypes.byref(m) for m in ms]))
         return (v.value, t.value) + tuple(m.value for m in ms)
 
     def fp32_set_kernel(self, nrhs, variant, rhs_tile=0):
         """Fix the FP32 operator for an RHS count (0 per-receiver, 1 bucketed, 2 pair-symmetric, 3 pair-symmetric
-        with two warps per receiver, 4 tensor cores with rhs_tile = nrhs)."""
+        with two warps per receiver, 4 tensor cores and 5 pair-symmetric tensor cores with rhs_tile = nrhs)."""
         check(lib().sg_fp32_set_kernel(self.h, int(nrhs), int(variant), int(rhs_tile)))
 
     def tc_set_window(self, emitters):

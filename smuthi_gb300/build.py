@@ -15,7 +15,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsmuthi_gb300.so")
 SOURCES = ["sg_coupling.cu", "sg_gmres.cu", "sg_capi.cu", "sg_peak.cu", "sg_noalloc.cu", "sg_bucket.cu",
            "sg_precond.cu", "sg_tc.cu", "sg_table.cu", "sg_farfield.cu", "sg_volume.cu",
-           "sg_nearfield.cu", "sg_sym.cu"]
+           "sg_nearfield.cu", "sg_sym.cu", "sg_tcsym.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3", "--expt-relaxed-constexpr",
          "-I", os.path.join(HERE, os.pardir, "include")]

@@ -594,17 +594,18 @@ int sg_measure_fma_peak(sg_context *ctx, int precision, double *tflops) {
 }
 
 int sg_fp32_autotune(sg_context *ctx, int nrhs, int *variant, int *rhs_tile, double *ms_receiver,
-                     double *ms_bucket, double *ms_symmetric, double *ms_tensor) {
+                     double *ms_bucket, double *ms_symmetric, double *ms_tensor, double *ms_tensor_symmetric) {
   return guarded([&]() -> int {
     SG_REQUIRE(ctx && variant, "null argument");
     for (const auto &t : ctx->tuned)
       if (t.nrhs == nrhs) {
         *variant = t.variant;
-        if (rhs_tile) *rhs_tile = t.variant == 4 ? nrhs : (t.variant >= 2 ? t.sym_rt : t.rt);
+        if (rhs_tile) *rhs_tile = t.variant >= 4 ? nrhs : (t.variant >= 2 ? t.sym_rt : t.rt);
         if (ms_receiver) *ms_receiver = t.ms_receiver;
         if (ms_bucket) *ms_bucket = t.ms_bucket;
         if (ms_symmetric) *ms_symmetric = t.ms_sym;
         if (ms_tensor) *ms_tensor = t.ms_tc;
+        if (ms_tensor_symmetric) *ms_tensor_symmetric = t.ms_tcs;
         return SG_OK;
       }
     *variant = -1;
@@ -626,10 +627,10 @@ int sg_fp32_set_kernel(sg_context *ctx, int nrhs, int variant, int rhs_tile) {
     SG_REQUIRE(ctx, "null context");
     SG_REQUIRE(nrhs >= 1, "nrhs must be >= 1");
     SG_REQUIRE(!ctx->vol && ctx->kind >= 0, "a radial lookup must be set");
-    SG_REQUIRE(variant >= 0 && variant <= 4, "variant must be 0, 1, 2, 3 or 4");
+    SG_REQUIRE(variant >= 0 && variant <= 5, "variant must be 0, 1, 2, 3, 4 or 5");
     use_device(ctx);
     ensure_pairs(ctx, ctx->stream);  // builds the FP32 operator data now (it would clear the choice later)
-    sg_context::Tuned t{nrhs, variant, 0, -1.f, -1.f, 0, -1.f, -1.f};
+    sg_context::Tuned t{nrhs, variant, 0, -1.f, -1.f, 0, -1.f, -1.f, -1.f};
     if (variant == 0) {
       SG_REQUIRE(rhs_tile == 1 || rhs_tile == 2 || rhs_tile == 4 || rhs_tile == 8 || rhs_tile == 16,
                  "per-receiver RHS tile must be 1, 2, 4, 8 or 16");
@@ -640,6 +641,10 @@ int sg_fp32_set_kernel(sg_context *ctx, int nrhs, int variant, int rhs_tile) {
     } else if (variant == 4) {
       SG_REQUIRE(sg::tc_supported(ctx, nrhs), "the tensor-core operator needs blocksize <= 48 and nrhs in {16, 32, 64}");
       SG_REQUIRE(rhs_tile == nrhs, "the tensor-core operator takes all right-hand sides at once (rhs_tile = nrhs)");
+    } else if (variant == 5) {
+      SG_REQUIRE(sg::tcsym_supported(ctx, nrhs),
+                 "the pair-symmetric tensor-core operator needs blocksize <= 32 and nrhs in {16, 32}");
+      SG_REQUIRE(rhs_tile == nrhs, "the tensor-core operators take all right-hand sides at once (rhs_tile = nrhs)");
     } else {
       SG_REQUIRE(sg::sym_supported(ctx), "the pair-symmetric kernel needs blocksize <= 64");
       SG_REQUIRE(rhs_tile >= 1 && rhs_tile <= sg::sym_max_tile(ctx) && (rhs_tile & (rhs_tile - 1)) == 0,

@@ -1126,8 +1126,10 @@ static int autotune_fp32(sg_context *c, const double2 *x, double2 *y, int R, boo
     }
   }
   // the tensor-core operator (3xTF32, accumulators drained every few emitters)
-  float ms_tc = -1.f;
+  float ms_tc = -1.f, ms_tcs = -1.f;
   if (tc_supported(c, R)) ms_tc = time_it([&] { c->launches += launch_tc_matvec(c, x, y, R, master, st); });
+  if (tcsym_supported(c, R))
+    ms_tcs = time_it([&] { c->launches += launch_tcsym_matvec(c, x, y, R, master, st); });
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   int v = 0;
@@ -1140,8 +1142,12 @@ static int autotune_fp32(sg_context *c, const double2 *x, double2 *y, int R, boo
     v = sym_split == 2 ? 3 : 2;
     best = ms_sym;
   }
-  if (ms_tc >= 0.f && ms_tc < best) v = 4;
-  c->tuned.push_back({R, v, best_rt, best_rec, ms_bucket, sym_rt, ms_sym, ms_tc});
+  if (ms_tc >= 0.f && ms_tc < best) {
+    v = 4;
+    best = ms_tc;
+  }
+  if (ms_tcs >= 0.f && ms_tcs < best) v = 5;
+  c->tuned.push_back({R, v, best_rt, best_rec, ms_bucket, sym_rt, ms_sym, ms_tc, ms_tcs});
   return v;
 }
 
@@ -1170,7 +1176,9 @@ void apply_padded(sg_context *c, const double2 *x, double2 *y, int R, bool maste
       sym_rt = c->tuned.back().sym_rt;
     }
   }
-  if (variant == 4) {
+  if (variant == 5) {
+    c->launches += launch_tcsym_matvec(c, x, y, R, master, st);
+  } else if (variant == 4) {
     c->launches += launch_tc_matvec(c, x, y, R, master, st);
   } else if (variant == 2 || variant == 3) {
     c->launches += launch_sym_matvec(c, x, y, R, master, sym_rt, variant == 3 ? 2 : 1, st);

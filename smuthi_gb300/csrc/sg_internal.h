@@ -93,6 +93,8 @@ void k_to_df64(const double2 *x, void *xdf, size_t n, cudaStream_t st);
 bool tc_supported(const sg_context *c, int R);
 int launch_tc_matvec(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st);
 bool tc_check_error(sg_context *c, cudaStream_t st);  // reads and clears the timeout flag (synchronises)
+bool tcsym_supported(const sg_context *c, int R);
+int launch_tcsym_matvec(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st);
 // FP32 W x in c->sym_yacc -> FP64 W x or x - T (W x) (diagonal or dense T); one launch
 void launch_fp32_epilogue(sg_context *c, const double2 *x, double2 *y, int R, bool master, cudaStream_t st);
 // y = M x or W x in double-float arithmetic (FP64-grade; builds the df64 coefficients on first use)
@@ -217,6 +219,9 @@ struct sg_context {
   bool df_ready = false;
   sg::DevBuf<double2> xdf;  // double-float copy of the operator input (16 bytes per complex)
   sg::DevBuf<float> tc_xop;  // tensor-core operator: pre-split TF32 hi/lo RHS panels
+  sg::DevBuf<float> tc_xops;  // pair-symmetric tensor-core operator: the same panels of S x
+  sg::DevBuf<int4> tcs_items; // pair-symmetric tensor-core operator: (receiver pair, emitter run)
+  int tcs_n_items = 0, tcs_items_n = -1;
   sg::DevBuf<int> tc_err;    // tensor-core operator: set when a bounded wait ran out
   bool tc_err_init = false;
   int tc_win = 8;            // tensor-core operator: emitters per accumulator before it is drained
@@ -237,12 +242,13 @@ struct sg_context {
   // pair-symmetric kernel
   struct Tuned {
     int nrhs, variant;  // 0 per-receiver, 1 bucketed, 2 pair-symmetric, 3 pair-symmetric (2 warps per receiver),
-                        // 4 tensor cores (3xTF32)
+                        // 4 tensor cores (3xTF32), 5 pair-symmetric tensor cores
     int rt;             // per-receiver kernel: RHS tile per CTA
     float ms_receiver, ms_bucket;  // best per-receiver tile, bucketed (< 0: not a candidate)
     int sym_rt;         // pair-symmetric kernel: RHS tile per CTA
     float ms_sym;       // best pair-symmetric tile and layout (< 0: not a candidate)
     float ms_tc;        // tensor-core operator (< 0: not a candidate)
+    float ms_tcs;       // pair-symmetric tensor-core operator (< 0: not a candidate)
   };
   std::vector<Tuned> tuned;
   std::vector<std::pair<int, int>> tuned_df;  // double-float kernel: (nrhs, RHS tile)

@@ -96,7 +96,8 @@ def main(argv=None):
                     help="time the near field of a plane-wave expansion at this many points instead")
     ap.add_argument("--fp32-kernel", default=None, metavar="VARIANT:TILE",
                     help="fix the FP32 kernel (0 per-receiver, 1 bucketed, 2 pair-symmetric, 3 pair-symmetric "
-                         "with two warps per receiver, 4 tensor cores with tile = nrhs) and its RHS tile "
+                         "with two warps per receiver, 4 tensor cores, 5 pair-symmetric tensor cores, tile = nrhs "
+                         "for 4 and 5) and its RHS tile "
                          "instead of the autotuner's choice")
     a = ap.parse_args(argv)
     if a.nearfield:
@@ -129,7 +130,7 @@ def main(argv=None):
         out["table_shape"] = system["table_shape"]
     if a.precision == "fp32" and not a.volume:
         out["fp32_kernel"] = dict(zip(("variant", "rhs_tile", "ms_per_receiver", "ms_bucketed", "ms_symmetric",
-                                       "ms_tensor_core"),
+                                       "ms_tensor_core", "ms_tensor_core_symmetric"),
                                       ctx.fp32_autotune(a.nrhs)))
     print(json.dumps(out))
     ctx.close()

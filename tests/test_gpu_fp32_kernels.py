@@ -3,8 +3,8 @@
 The FP32 operator drives the correction solves of the mixed-precision refinement; the autotuner
 picks among the per-receiver kernel (RHS tiles 1-16), the interval-bucketed kernel and the
 pair-symmetric kernel (one interpolation per unordered pair for both directions, with one or two warps
-per receiver). The tensor-core operator (variant 4: tcgen05 3xTF32 with drained
-accumulators) is held to the same bound. Each is fixed
+per receiver). The tensor-core operators (variant 4: tcgen05 3xTF32 with drained
+accumulators; variant 5: the same with one interpolated block per unordered pair) are held to the same bound. Each is fixed
 here with ``fp32_set_kernel`` and compared, through the C ABI, with the FP64 operator (relative
 2-norm 2e-5, the FP32 bound the other FP32 tests use) and with the reference's W x / M x.
 Also: the full (non-diagonal) T-matrix epilogue of the FP64, per-receiver FP32 and pair-symmetric
@@ -28,6 +28,8 @@ def _variants(ctx, R, bs):
     out += [(3, t) for t in (4, 8, 16) if R % t == 0 and t <= (16 if bs <= 32 else 8)]
     if R in (16, 32, 64) and bs <= 48:
         out.append((4, R))
+    if R in (16, 32) and bs <= 32:
+        out.append((5, R))
     return out
 
 
@@ -81,7 +83,7 @@ def test_full_t_epilogue(name, gpu_context):
         wx = gpu_context.coupling_matvec(X, _lib.SG_FP64).reshape(n, bs, R)
         ref = (Xr - np.einsum("iab,ibr->iar", blocks[types], wx)).reshape(X.shape)
         assert gc.relerr(gpu_context.master_matvec(X, _lib.SG_FP64), ref) < 1e-13
-        for v, t in [(0, 1), (2, 1)] + ([(0, 4), (2, 4), (3, 4)] if R == 4 else []) + ([(4, 16)] if R == 16 else []):
+        for v, t in [(0, 1), (2, 1)] + ([(0, 4), (2, 4), (3, 4)] if R == 4 else []) + ([(4, 16), (5, 16)] if R == 16 else []):
             gpu_context.fp32_set_kernel(R, v, t)
             assert gc.relerr(gpu_context.master_matvec(X, _lib.SG_FP32), ref) < TOL32, (R, v, t)
 
@@ -90,7 +92,8 @@ def test_fp32_set_kernel_rejects_bad_choices(gpu_context):
     from smuthi_gb300 import _lib
     g = gc.load("c1")
     _product_system(g, "linear", gpu_context)
-    for args in [(16, 0, 3), (4, 0, 8), (16, 2, 32), (6, 2, 4), (4, 5, 1), (2, 3, 2), (8, 4, 8), (16, 4, 8)]:
+    for args in [(16, 0, 3), (4, 0, 8), (16, 2, 32), (6, 2, 4), (4, 6, 1), (2, 3, 2), (8, 4, 8), (16, 4, 8), (64, 5, 64),
+                 (16, 5, 8)]:
         with pytest.raises(_lib.SmuthiGB300Error) as e:
             gpu_context.fp32_set_kernel(*args)
         assert e.value.code == _lib.SG_ERR_ARG
@@ -117,6 +120,9 @@ def test_full_size_c2_symmetric_kernel(gpu_context):
     ys = gpu_context.coupling_matvec(X, _lib.SG_FP32)
     gpu_context.fp32_set_kernel(16, 3, 16)
     assert gc.relerr(gpu_context.coupling_matvec(X, _lib.SG_FP32), y64) < TOL32
+    for v in (4, 5):
+        gpu_context.fp32_set_kernel(16, v, 16)
+        assert gc.relerr(gpu_context.coupling_matvec(X, _lib.SG_FP32), y64) < 5e-6, v
     gpu_context.fp32_set_kernel(16, 0, 8)
     yr = gpu_context.coupling_matvec(X, _lib.SG_FP32)
     assert gc.relerr(ys, y64) < TOL32
@@ -126,8 +132,8 @@ def test_full_size_c2_symmetric_kernel(gpu_context):
                                             interpolator_kind="cubic", context=gpu_context)
     yt = gpu_context.coupling_matvec(X, _lib.SG_FP32)
     assert gc.relerr(yt, y64) < TOL32
-    variant, tile, ms_rec, ms_bucket, ms_sym, ms_tc = gpu_context.fp32_autotune(16)
-    assert variant in (0, 1, 2, 3, 4) and ms_rec > 0 and ms_sym > 0 and ms_tc > 0
+    variant, tile, ms_rec, ms_bucket, ms_sym, ms_tc, ms_tcs = gpu_context.fp32_autotune(16)
+    assert variant in (0, 1, 2, 3, 4, 5) and ms_rec > 0 and ms_sym > 0 and ms_tc > 0 and ms_tcs > 0
     del W2
 
 
