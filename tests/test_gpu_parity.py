@@ -294,10 +294,11 @@ def test_tensor_core_operator_matches_fp64(name, gpu_context):
             assert gc.relerr(tc, ref) < 5e-6, (R, fn.__name__, gc.relerr(tc, ref))
 
 
-@pytest.mark.parametrize("count", [1, 2])
+@pytest.mark.parametrize("count", [1, 2, 3, 5])
 def test_one_and_two_particle_systems(count, gpu_context):
-    """Smallest systems (the self pair only, one pair): every precision against the oracle's FP64
-    operator, and the plain and chosen solves to their tolerances."""
+    """Smallest systems (the self pair only, one pair, odd counts whose last receiver pair has one
+    particle): every precision against the oracle's FP64 operator, both tensor-core operators on 16
+    RHS, and the plain and chosen solves to their tolerances."""
     from smuthi_gb300 import _lib
     g = gc.load("c5s")
     sub = {k: g[k] for k in g}
@@ -312,6 +313,12 @@ def test_one_and_two_particle_systems(count, gpu_context):
     assert gc.relerr(W.linear_operator.matvec(x), ref) < 1e-12
     assert gc.relerr(gpu_context.coupling_matvec(x, _lib.SG_DF64), ref) < 1e-12
     assert gc.relerr(gpu_context.coupling_matvec(x, _lib.SG_FP32), ref) < 1e-5
+    X = np.ascontiguousarray(np.stack([x * np.exp(0.3j * q) for q in range(16)], axis=1))
+    Y = np.stack([Wo.matvec(X[:, q]) for q in range(16)], axis=1)
+    assert gc.relerr(gpu_context.coupling_matvec(X, _lib.SG_TF32X3), Y) < 5e-6
+    if count >= 2:
+        gpu_context.fp32_set_kernel(16, 5, 16)
+        assert gc.relerr(gpu_context.coupling_matvec(X, _lib.SG_FP32), Y) < 5e-6
     b = np.ascontiguousarray(x)
     for prec, tol in ((_lib.SG_FP64, 1e-12), (_lib.SG_FP32 | _lib.SG_DF64, 1e-6)):
         sol, info = gpu_context.gmres(b, np.zeros_like(b), tol, precision=prec)
