@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(TcShape<BP, R>::THREADS, 1) tc_coupling_kernel
     const size_t plane = (size_t)bs2, block = (size_t)NC * bs2;
     int4 pd_next = gvalid ? __ldg(&a.pairs[(size_t)gi * N]) : make_int4(0, 0, 0x3f800000, 0);
     for (int jj = 0; jj < N; ++jj) {
-      if (__shfl_sync(kTcFull, *abort_flag, 0)) break;  // one verdict per warp
+      if (__shfl_sync(kTcFull, *abort_flag, 0)) break;  // one decision per warp
       const int s = jj % S, q = jj / S;
       const int4 pd = pd_next;
       if (jj + 1 < N && gvalid) pd_next = __ldg(&a.pairs[(size_t)gi * N + jj + 1]);
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(TcShape<BP, R>::THREADS, 1) tc_coupling_kernel
     // ------------------------------------------------------------------ drain (warps 0-3)
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
     for (int w = 0; w < nwin; ++w) {
-      if (__shfl_sync(kTcFull, *abort_flag, 0)) break;  // one verdict per warp
+      if (__shfl_sync(kTcFull, *abort_flag, 0)) break;  // one decision per warp
       const int b = w & 1;
       if (!tc_waitw(smem_u32(&acc_full[b]), (uint32_t)((w >> 1) & 1))) {
         if (lane == 0) {

@@ -64,7 +64,7 @@ __device__ __forceinline__ bool tc_wait1(uint32_t bar, uint32_t parity) {
   return true;
 }
 
-// whole warp: every lane polls (each gets the barrier's acquire); one verdict for the warp
+// whole warp: every lane polls (each gets the barrier's acquire); one decision for the warp
 __device__ __forceinline__ bool tc_waitw(uint32_t bar, uint32_t parity) {
   const long long t0 = clock64();
   while (true) {
