@@ -242,6 +242,19 @@ int sg_bessel_jac_table(sg_context *ctx, const void *kappa, const void *jac, int
 int sg_lookup_contract(sg_context *ctx, const void *a, int nr, int nk, const void *g, int ncols, const int *cols,
                        double factor_re, double factor_im, void *out, long long out_stride, void *stream);
 
+/* Regular spherical-wave coefficients of plane waves at points (the initial field at every particle
+ * for a batch of plane waves; the reference converts each wave per particle on the host:
+ * smuthi/initial_field.py:284-329 through smuthi/fields/transformations.py:77-131):
+ *   out[q][p][n] = sum_c amp[q][c][n] exp(i (kx (x_p - x0) + ky (y_p - y0) + kz (z_p - z0)))
+ * with kr[q][c] = (kx, ky, Re kz, Im kz, x0, y0, z0) for the plane-wave components c (at most 4) of
+ * wave q in the points' layer, and amp[q][c][n] the per-index factors of the transformation
+ * (4 sum_pol B^dagger(n, pol) e^{-i m alpha} g_pol). Device buffers: xyz float64[n_points][3],
+ * kr float64[nwaves][ncomp][7], amp complex128[nwaves][ncomp][blocksize],
+ * out complex128[nwaves][n_points][blocksize]. FP64; synchronous on `stream` (NULL = the context's
+ * stream). */
+int sg_plane_wave_swe(sg_context *ctx, int n_points, const void *xyz, int nwaves, int ncomp, const void *kr,
+                      int blocksize, const void *amp, void *out, void *stream);
+
 /* Particle sum of the scattered field's plane-wave expansion for the cross sections (the reference
  * converts each particle's expansion on the host: smuthi/postprocessing/far_field.py:363-427,
  * smuthi/postprocessing/scattered_field.py:80-150, smuthi/fields/transformations.py:133-233):

@@ -31,7 +31,7 @@ EXPORTS = ("sg_last_error", "sg_version", "sg_create", "sg_destroy", "sg_set_par
            "sg_tc_set_window", "sg_coupling_matvec_linear_noalloc", "sg_precond_param_count", "sg_precond_add_graph",
            "sg_precond_select", "sg_precond_clear", "sg_precond_set_params", "sg_precond_get_params",
            "sg_precond_apply_dev", "sg_precond_train_step", "sg_precond_export_blocks", "sg_bessel_jac_table",
-           "sg_lookup_contract",
+           "sg_lookup_contract", "sg_plane_wave_swe",
            "sg_farfield_sum", "sg_set_volume_lookup", "sg_farfield_sum_heights", "sg_pwe_field")
 
 
@@ -91,6 +91,7 @@ def _declare(L):
                              ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D)],
         "sg_fp32_set_kernel": [_P, _I, _I, _I],
         "sg_tc_set_window": [_P, _I],
+        "sg_plane_wave_swe": [_P, _I, _P, _I, _I, _P, _I, _P, _P, _P],
         "sg_coupling_matvec_linear_noalloc": [_I, _I, _P, _I, _P, _I, _D, _D, _P, _P, _P, _I, _P],
         "sg_bessel_jac_table": [_P, _P, _P, _I, _P, _I, _I, _P, _P],
         "sg_lookup_contract": [_P, _P, _I, _I, _P, _I, _P, _D, _D, _P, ctypes.c_longlong, _P],
@@ -349,6 +350,12 @@ class Context:
                                             ctypes.c_void_p(kpar_ptr), ctypes.c_void_p(S_ptr), int(na),
                                             ctypes.c_void_p(alpha_ptr), ctypes.c_void_p(zphase_ptr or 0),
                                             ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream or 0)))
+
+    def plane_wave_swe_dev(self, n_points, xyz_ptr, nwaves, ncomp, kr_ptr, blocksize, amp_ptr, out_ptr, stream=None):
+        """Device regular SWE coefficients of plane waves at points (see ``sg_plane_wave_swe``)."""
+        check(lib().sg_plane_wave_swe(self.h, int(n_points), ctypes.c_void_p(xyz_ptr), int(nwaves), int(ncomp),
+                                      ctypes.c_void_p(kr_ptr), int(blocksize), ctypes.c_void_p(amp_ptr),
+                                      ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream or 0)))
 
     def launch_count(self):
         n = ctypes.c_int64()

@@ -725,6 +725,18 @@ int sg_pwe_field(sg_context *ctx, int field, int n_points, const void *x, const 
   });
 }
 
+int sg_plane_wave_swe(sg_context *ctx, int n_points, const void *xyz, int nwaves, int ncomp, const void *kr,
+                      int blocksize, const void *amp, void *out, void *stream) {
+  return guarded([&]() -> int {
+    SG_REQUIRE(ctx && xyz && kr && amp && out, "null argument");
+    use_device(ctx);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    ctx->launches += sg::plane_wave_swe(n_points, (const double *)xyz, nwaves, ncomp, (const double *)kr, blocksize,
+                                        (const double2 *)amp, (double2 *)out, st);
+    return SG_OK;
+  });
+}
+
 int sg_precond_param_count(int blocksize) {
   if (blocksize < 1 || blocksize > 64) return -1;
   return sg::precond_param_count(blocksize);

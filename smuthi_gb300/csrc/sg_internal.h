@@ -165,6 +165,9 @@ void build_volume_table(int kind, const double2 *raw, int len_rho, int len_z, in
 int launch_volume(sg_context *c, const double2 *x, double2 *y, int R, bool master, bool fp32, cudaStream_t st);
 
 // field of a plane-wave expansion at points (sg_nearfield.cu); synchronous, returns kernels launched
+// regular SWE coefficients of plane waves at points (device buffers); returns the number of launches
+int plane_wave_swe(int np, const double *xyz, int nq, int nc, const double *kr, int bs, const double2 *amp,
+                   double2 *out, cudaStream_t st);
 int pwe_field(int field, int np, const double *x, const double *y, const double *z, int nk, const double2 *kp,
               const double2 *kz, int na, const double *alpha, const double2 *g, double2 k, double omega, double2 *out,
               cudaStream_t st);

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "sg_internal.h"
@@ -188,6 +189,56 @@ int pwe_field(int field, int np, const double *x, const double *y, const double 
   SG_CUDA(cudaGetLastError());
   SG_CUDA(cudaStreamSynchronize(st));  // the scratch buffers are released on return
   return 3;
+}
+
+// ------------------------------------------------------------------ plane waves -> regular SWE at points
+// out[q][p][n] = sum_c amp[q][c][n] exp(i (kx (x_p - x0) + ky (y_p - y0) + kz (z_p - z0))) for the
+// discrete plane-wave components c of wave q (wavevector kx, ky real, kz complex; reference point
+// r0), i.e. the regular spherical-wave coefficients of every wave at every point, the closed-form
+// PVWF -> SVWF transformation of a single plane-wave component. The per-n factors amp carry the
+// angular part (smuthi/fields/transformations.py:77-131 with one k point) and are formed by the
+// caller; this is the particle-dependent part. One thread per (wave, point); FP64.
+static constexpr int kPwsMaxComponents = 4;
+
+__global__ void plane_wave_swe_kernel(const double *xyz, int np, int nq, int nc, const double *kr, int bs,
+                                      const double2 *amp, double2 *out) {
+  const size_t total = (size_t)nq * np;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int q = (int)(e / np), p = (int)(e - (size_t)q * np);
+    const double x = xyz[3 * (size_t)p], y = xyz[3 * (size_t)p + 1], z = xyz[3 * (size_t)p + 2];
+    double2 ph[kPwsMaxComponents];
+    for (int c = 0; c < nc; ++c) {
+      const double *w = kr + ((size_t)q * nc + c) * 7;
+      const double dz = z - w[6];
+      const double arg = w[0] * (x - w[4]) + w[1] * (y - w[5]) + w[2] * dz;
+      const double damp = exp(-w[3] * dz);
+      double sn, cs;
+      sincos(arg, &sn, &cs);
+      ph[c] = make_double2(damp * cs, damp * sn);
+    }
+    double2 *o = out + e * bs;
+    for (int n = 0; n < bs; ++n) {
+      double re = 0.0, im = 0.0;
+      for (int c = 0; c < nc; ++c) {
+        const double2 a = amp[((size_t)q * nc + c) * bs + n];
+        re = fma(a.x, ph[c].x, fma(-a.y, ph[c].y, re));
+        im = fma(a.x, ph[c].y, fma(a.y, ph[c].x, im));
+      }
+      o[n] = make_double2(re, im);
+    }
+  }
+}
+
+int plane_wave_swe(int np, const double *xyz, int nq, int nc, const double *kr, int bs, const double2 *amp,
+                   double2 *out, cudaStream_t st) {
+  SG_REQUIRE(np >= 1 && nq >= 1 && bs >= 1, "plane-wave SWE: sizes must be positive");
+  SG_REQUIRE(nc >= 1 && nc <= kPwsMaxComponents, "plane-wave SWE: 1 to 4 plane-wave components per wave");
+  const size_t total = (size_t)nq * np;
+  const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, (size_t)sm_count() * 8);
+  plane_wave_swe_kernel<<<grid, 256, 0, st>>>(xyz, np, nq, nc, kr, bs, amp, out);
+  SG_CUDA(cudaGetLastError());
+  SG_CUDA(cudaStreamSynchronize(st));
+  return 1;
 }
 
 }  // namespace sg

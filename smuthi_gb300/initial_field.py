@@ -92,23 +92,13 @@ class PlaneWave:
         """
         positions = np.atleast_2d(np.asarray(positions, dtype=float))
         layer = layer_system.layer_number(positions[0, 2])
-        tau, ll, mm = flds.index_table(l_max, m_max)
-        out = np.zeros((len(positions), len(tau)), complex)
+        out = np.zeros((len(positions), flds.blocksize(l_max, m_max)), complex)
         for pwe in self.plane_wave_expansion(layer_system, layer):
-            k = pwe.k
-            kp = pwe.k_parallel
-            a = pwe.azimuthal_angle
-            kz = pwe.k_z()
-            _, pilm, taulm = legendre_normalized(kz / k, kp / k, l_max)
-            # per-n factor 4 sum_pol Bdag(n, pol) e^{-i m a} g_pol; the particle phase separates
-            d = positions - np.array(pwe.reference_point)[None, :]
-            ejkr = np.exp(1j * (kp * np.cos(a) * d[:, 0] + kp * np.sin(a) * d[:, 1] + kz * d[:, 2]))
-            for n in range(len(tau)):
-                acc = np.zeros(len(positions), complex)
-                for pol in range(2):
-                    bd = transformation_coefficients_vwf(tau[n], ll[n], mm[n], pol, pilm, taulm, dagger=True)[0]
-                    acc += bd * (np.exp(-1j * mm[n] * a) * (pwe.coefficients[pol] * ejkr))
-                out[:, n] += 4 * acc
+            kr, amp = component_terms(pwe, l_max, m_max)
+            # the per-n factor amp (4 sum_pol Bdag(n, pol) e^{-i m a} g_pol) and the particle phase separate
+            d = positions - kr[4:7][None, :]
+            ejkr = np.exp(1j * (kr[0] * d[:, 0] + kr[1] * d[:, 1] + complex(kr[2], kr[3]) * d[:, 2]))
+            out += ejkr[:, None] * amp[None, :]
         return out
 
     def spherical_wave_expansion(self, particle, layer_system):
@@ -120,3 +110,55 @@ class PlaneWave:
         swe.coefficients = self.swe_coefficients([particle.position], layer_system, particle.l_max,
                                                  particle.m_max)[0]
         return swe
+
+
+def component_terms(pwe, l_max, m_max):
+    """Wavevector row and per-index factors of one discrete plane-wave component.
+
+    Returns kr = [kx, ky, Re kz, Im kz, x0, y0, z0] (reference point r0) and amp[n] =
+    4 sum_pol B^dagger(n, pol) e^{-i m alpha} g_pol, so that the component's regular SWE coefficient
+    at a point r is amp[n] exp(i k . (r - r0)) (smuthi/fields/transformations.py:77-131, one k point).
+    """
+    k, kp, a = pwe.k, pwe.k_parallel, pwe.azimuthal_angle
+    kz = complex(pwe.k_z())
+    _, pilm, taulm = legendre_normalized(kz / k, kp / k, l_max)
+    tau, ll, mm = flds.index_table(l_max, m_max)
+    amp = np.zeros(len(tau), complex)
+    for n in range(len(tau)):
+        for pol in range(2):
+            bd = transformation_coefficients_vwf(tau[n], ll[n], mm[n], pol, pilm, taulm, dagger=True)[0]
+            amp[n] += 4 * bd * (np.exp(-1j * mm[n] * a) * pwe.coefficients[pol])
+    kpr = float(np.real(kp))
+    r0 = pwe.reference_point
+    kr = np.array([kpr * np.cos(a), kpr * np.sin(a), kz.real, kz.imag, r0[0], r0[1], r0[2]], float)
+    return kr, amp
+
+
+def swe_coefficients_batch(fields, positions, layer_system, l_max, m_max, context):
+    """Regular SWE coefficients [len(fields), N, blocksize] of plane waves at positions in one layer.
+
+    The per-wave factors are formed here (O(blocksize) per plane-wave component); the particle-dependent
+    part runs on the context's GPU (``sg_plane_wave_swe``, FP64). Falls back to the host for
+    evanescent in-plane wavenumbers (complex k_parallel), which the kernel does not take.
+    """
+    import torch
+    positions = np.atleast_2d(np.asarray(positions, dtype=float))
+    layer = layer_system.layer_number(positions[0, 2])
+    comps = [f.plane_wave_expansion(layer_system, layer) for f in fields]
+    if any(np.iscomplexobj(c.k_parallel) and np.imag(c.k_parallel) != 0 for cs in comps for c in cs):
+        return np.stack([f.swe_coefficients(positions, layer_system, l_max, m_max) for f in fields])
+    nc = max(len(cs) for cs in comps)
+    bs = flds.blocksize(l_max, m_max)
+    kr = np.zeros((len(fields), nc, 7))
+    amp = np.zeros((len(fields), nc, bs), complex)
+    for q, cs in enumerate(comps):
+        for c, pwe in enumerate(cs):
+            kr[q, c], amp[q, c] = component_terms(pwe, l_max, m_max)
+    dev = torch.device("cuda", context.device)
+    xyz_t = torch.from_numpy(np.ascontiguousarray(positions)).to(dev)
+    kr_t = torch.from_numpy(kr).to(dev)
+    amp_t = torch.from_numpy(amp).to(dev)
+    out_t = torch.empty((len(fields), len(positions), bs), dtype=torch.complex128, device=dev)
+    context.plane_wave_swe_dev(len(positions), xyz_t.data_ptr(), len(fields), nc, kr_t.data_ptr(), bs,
+                               amp_t.data_ptr(), out_t.data_ptr())
+    return out_t.cpu().numpy()

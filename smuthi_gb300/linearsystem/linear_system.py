@@ -308,22 +308,31 @@ class LinearSystem:
         sys.stdout.write('Number of unknowns: %i\n' % SystemMatrix(particle_list).shape[0])
 
     def prepare(self):
-        self.compute_initial_field_coefficients()
+        # the coupling matrix first: its GPU context also evaluates the initial fields at the particles
         self.compute_t_matrix()
         self.compute_coupling_matrix()
+        self.compute_initial_field_coefficients(context=getattr(self.coupling_matrix, 'context', None))
         self.master_matrix = MasterMatrix(t_matrix=self.t_matrix, coupling_matrix=self.coupling_matrix)
 
-    def compute_initial_field_coefficients(self):
+    def compute_initial_field_coefficients(self, context=None):
         """Regular SWE of every initial field at every particle (``p.initial_fields``; ``p.initial_field``
-        is the first)."""
+        is the first). With a GPU context and plane-wave initial fields, all waves of a particle group are
+        evaluated in one call of ``sg_plane_wave_swe``."""
+        from ..initial_field import PlaneWave, swe_coefficients_batch
         groups = {}
         for i, p in enumerate(self.particle_list):
             groups.setdefault((p.l_max, p.m_max, self.layer_system.layer_number(p.position[2])), []).append(i)
             p.initial_fields = [None] * len(self.initial_fields)
+        batch = {}
+        if context is not None and all(isinstance(f, PlaneWave) for f in self.initial_fields):
+            for key, idx in groups.items():
+                pos = np.array([self.particle_list[i].position for i in idx], dtype=float)
+                batch[key] = swe_coefficients_batch(self.initial_fields, pos, self.layer_system, key[0], key[1],
+                                                    context)
         for q, field in enumerate(self.initial_fields):
             for (lm, mm, layer), idx in groups.items():
                 pos = np.array([self.particle_list[i].position for i in idx], dtype=float)
-                coef = field.swe_coefficients(pos, self.layer_system, lm, mm)
+                coef = batch[(lm, mm, layer)][q] if batch else field.swe_coefficients(pos, self.layer_system, lm, mm)
                 k = field.angular_frequency() * self.layer_system.refractive_indices[layer]
                 for row, i in enumerate(idx):
                     p = self.particle_list[i]
