@@ -54,6 +54,8 @@ def test_fp32_kernels_match_fp64_and_reference(name, gpu_context):
             X = _rhs(x, R, 7)
             y64 = gpu_context.coupling_matvec(X, _lib.SG_FP64)
             m64 = gpu_context.master_matvec(X, _lib.SG_FP64)
+            # the double-float operator at the RHS tile its autotuner picks for R (4, 8 or 16)
+            assert gc.relerr(gpu_context.master_matvec(X, _lib.SG_DF64), m64) < 1e-12, (name, kind, R)
             for v, t in _variants(gpu_context, R, bs):
                 gpu_context.fp32_set_kernel(R, v, t)
                 y32 = gpu_context.coupling_matvec(X, _lib.SG_FP32)
@@ -117,6 +119,7 @@ def test_full_size_c2_symmetric_kernel(gpu_context):
     rng = np.random.default_rng(9)
     X = np.ascontiguousarray(rng.standard_normal((W.shape[0], 16)) + 1j * rng.standard_normal((W.shape[0], 16)))
     y64 = gpu_context.coupling_matvec(X, _lib.SG_FP64)
+    assert gc.relerr(gpu_context.coupling_matvec(X, _lib.SG_DF64), y64) < 1e-12
     gpu_context.fp32_set_kernel(16, 2, 16)
     ys = gpu_context.coupling_matvec(X, _lib.SG_FP32)
     gpu_context.fp32_set_kernel(16, 3, 16)
